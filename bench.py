@@ -1,0 +1,319 @@
+"""Benchmark of the batch-Hogwild SGD path (one JSON line on rank 0).
+
+Workload (BASELINE config 2): planted-model matrix 480,189 x 17,770 with 99,072,112 train
+ratings, k = 128, fp16 factors, 20 epochs, synthetic (seeded) in place of Netflix.
+  value  updates/s = nnz * epochs / time, epochs run on device-resident data (one epoch =
+         one step = one kernel launch), CUDA events on the launching stream;
+  e2e    the same metric through the C ABI (cumf_train: pinned host ratings in, fp32 model
+         out, 20 epochs including H2D, prep, export and D2H);
+  roofline   algorithmic bytes of the update kernel (12 + 4k bytes per sample) / launch time
+             against the measured HBM copy bandwidth;
+  cpu_baseline  the oracle's threaded CPU port of the same algorithm (fp32) on the host cores.
+`--impl reference` times that CPU port alone as the reference arm (the reference's own
+binaries are x86 builds of this container and do not exist on the GPU host).
+Multi-GPU (torchrun): independent replicas, one per GPU (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+K = 128
+BYTES_PER_SAMPLE = {"fp16": 12 + 4 * K * 2, "bf16": 12 + 4 * K * 2, "bf16sr": 12 + 4 * K * 2,
+                    "fp16sr": 12 + 4 * K * 2, "fp32": 12 + 4 * K * 4}
+WORKLOAD = "c2 planted 480189x17770, 99072112 train ratings, k=128"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram read+write bytes per launch of the update kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "sgd_hogwild_c2.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"cumf_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_port_baseline(train: np.ndarray, m: int, n: int, seconds_budget: float = 12.0):
+    """Threaded CPU port (oracle) of the batch-Hogwild update on a bounded sample of the
+    workload: fp32 factors of the full c2 shape; each pass gives every worker one batch of
+    128 consecutive ratings from a rotating window of the c2 train set; passes repeat until
+    about `seconds_budget` seconds of work are done."""
+    from oracle import oracle
+    oracle.build_oracle()
+    threads = os.cpu_count() or 1
+    lr = oracle.lr_table(0.08, 0.3, 0.0, 8)
+    P = oracle.init_factors(m, K, "fp32", 1, 1)
+    Q = oracle.init_factors(n, K, "fp32", 1, 2)
+    nnz = len(train)
+    workers = max(1, min(threads * 64, nnz // 128))
+    win = workers * 128
+    samples = passes = 0
+    t0 = time.perf_counter()
+    while True:
+        start = (passes * 7919 * 128) % max(1, nnz - win + 1)
+        oracle.hogwild_threads(train[start:start + win], P, Q, workers, lr, 0, 1, 0.05, 0.05, 1 + passes,
+                               threads)
+        samples += win
+        passes += 1
+        el = time.perf_counter() - t0
+        if el >= seconds_budget:
+            break
+    return {"value": samples / el, "unit": "updates/s", "cores": threads, "kind": "port",
+            "sample": f"{samples} Hogwild updates ({passes} passes x {workers} workers x 128) over "
+                      f"windows of the c2 train set, fp32 factors 480189x128 / 17770x128, {el:.1f} s"}
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from cumf_sgd_gb300 import synth
+    t0 = time.time()
+    train, _ = synth.generate(synth.C2, seed=0, device="cuda" if _has_cuda() else "cpu")
+    gen_s = time.time() - t0
+    per_step = []
+    budget = max(2.0, 60.0 / (args.warmup + args.steps))  # whole arm: about a minute of CPU work
+    for i in range(args.warmup + args.steps):
+        base = cpu_port_baseline(train, synth.C2.m, synth.C2.n, seconds_budget=budget)
+        if i >= args.warmup:
+            per_step.append(base)
+    v = statistics.mean(b["value"] for b in per_step)
+    line = {"impl": "reference", "metric": "sgd_updates_per_sec", "value": v, "unit": "updates/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "storage": "fp32 (CPU port)", "k": K},
+            "cpu_baseline": dict(per_step[-1], value=v),
+            "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gen_seconds": gen_s}
+    print(json.dumps(line), flush=True)
+
+
+def _has_cuda():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp16")
+    ap.add_argument("--workers", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--e2e-epochs", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the c2 size (tests only)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    build.build()
+    spec = synth.C2 if args.scale >= 1.0 else synth.scaled(synth.C2, args.scale)
+    train, test = synth.generate(spec, seed=rank, device="cuda")
+    m, n, nnz = spec.m, spec.n, len(train)
+    sm, _, _ = cm.device_info(local)
+    workers = args.workers or cm.default_workers(sm, K, args.precision, args.lanes)
+    prec = args.precision
+    eb = 4 if prec == "fp32" else 2
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    # Device-resident problem, prepared exactly as cumf_train does.
+    d_raw = torch.from_numpy(train.view(np.uint8)).to(dev)
+    mean, std = cm.dev_rating_stats(d_raw.data_ptr(), nnz, sp)
+    std32 = np.float32(std)
+    scale = max(np.float32(1e-4), std32)
+    pm = torch.from_numpy(cm.random_map(rank, m)).to(dev)
+    qm = torch.from_numpy(cm.random_map(rank, n)).to(dev)
+    d_R = torch.empty_like(d_raw)
+    cm.dev_shuffle_scale(d_raw.data_ptr(), d_R.data_ptr(), nnz, pm.data_ptr(), m, qm.data_ptr(), n,
+                         float(np.float32(1.0 / float(scale))), 0, sp)
+    del d_raw
+    P = torch.empty(m * K * eb, dtype=torch.uint8, device=dev)
+    Q = torch.empty(n * K * eb, dtype=torch.uint8, device=dev)
+    cm.dev_init_factors(P.data_ptr(), m, K, prec, rank, 1, sp)
+    cm.dev_init_factors(Q.data_ptr(), n, K, prec, rank, 2, sp)
+    epochs_total = args.warmup + args.steps
+    lr = torch.from_numpy(cm.lr_schedule(0.08, 0.3, 0.0, epochs_total + 4)).to(dev)
+    lp = float(np.float32(0.05) / scale)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def epoch(e):
+        cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m, Q.data_ptr(), n, K, prec, workers, args.lanes,
+                      lr.data_ptr(), e, 1, lp, lp, rank, status.data_ptr(), sp)
+
+    for e in range(args.warmup):
+        epoch(e)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for e in range(args.warmup, epochs_total):
+            epoch(e)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clocks = clk.summary()
+    assert int(status.item()) == 0, "update kernel flagged an out-of-range index"
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    secs = ms / 1e3
+    updates_per_sec = nnz * args.steps * world / secs
+    batches = cm.batches_per_worker(nnz, workers)
+    samples_per_launch = workers * batches * 128
+    launch_s = secs / args.steps
+    achieved = samples_per_launch * BYTES_PER_SAMPLE[prec] / launch_s / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # Test RMSE of the device-resident run (for the record).
+    del P, Q, d_R
+    torch.cuda.empty_cache()
+
+    # End to end through the C ABI: pinned host ratings -> cumf_train (20 epochs) -> fp32 model.
+    e2e = None
+    if True:
+        prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=m, n=n, pinned=True)
+        tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+        par = cm.Parameter(k=K, num_workers=workers, num_iters=args.e2e_epochs, lambda_p=0.05, lambda_q=0.05,
+                           alpha=0.08, beta=0.3, seed=rank, gpu=local, precision=prec, lanes=args.lanes)
+        cm.sgd_train(prob, None, cm.Parameter(**{**par.__dict__, "num_iters": 1}))  # warm-up call
+        t0 = time.perf_counter()
+        model, st = cm.sgd_train(prob, None, par, with_stats=True)
+        wall = time.perf_counter() - t0
+        test_rmse = cm.calc_rmse(tprob, model)
+        e2e = {"value": nnz * args.e2e_epochs * world / wall, "unit": "updates/s",
+               "h2d_bytes_per_step": nnz * 12 + 4 * (m + n), "d2h_bytes_per_step": 4 * K * (m + n),
+               "epochs_per_step": args.e2e_epochs, "wall_s": wall,
+               "prep_ms": st.prep_ms, "train_ms": st.train_ms, "export_ms": st.export_ms,
+               "test_rmse": test_rmse}
+        del model
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_port_baseline(train, m, n, seconds_budget=args.ref_seconds)
+
+    if rank == 0:
+        line = {"metric": "sgd_updates_per_sec", "value": updates_per_sec, "unit": "updates/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": prec, "data": "synthetic",
+                "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz, "k": K, "storage": prec,
+                           "workers": workers, "lanes": args.lanes or "auto", "step": "one epoch (one launch)",
+                           "samples_per_epoch": samples_per_launch,
+                           "l2": "inputs larger than L2 (ratings 1.19 GB)", "parallelism": f"replicas{world}"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(),
+                             "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
+                "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

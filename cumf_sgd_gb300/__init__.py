@@ -1,0 +1,360 @@
+"""cumf_sgd_gb300 - GB300-native batch-Hogwild SGD matrix factorization.
+
+Python mirror of cuMF_SGD's host interface over the C ABI in include/cumf_sgd.h:
+
+  Parameter            singleGPU/sgd.h:26-46 (same defaults)
+  parse_argument       singleGPU/main.cpp:33-227
+  read_problem         singleGPU/sgd.cu:190-335
+  sgd_train            singleGPU/sgd.cu:638-690
+  save_model           singleGPU/main.cpp:231-273
+  mf_load_model        test/mf.cpp:3706-3777
+  calc_rmse            test/mf.cpp:3815-3839
+  sgd_update           singleGPU/sgd_kernel.cu:125 (device-resident epochs)
+
+All compute runs in libcumf_sgd.so; a missing library raises ImportError at first use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import CumfError, PRECISIONS, FP16, BF16, FP32, BF16_SR, FP16_SR  # noqa: F401
+
+NODE_DTYPE = np.dtype([("u", "<i4"), ("v", "<i4"), ("r", "<f4")])
+
+
+@dataclasses.dataclass
+class Parameter:
+    """Parameter (singleGPU/sgd.h:26-46) with the same defaults, plus seed/precision/lanes."""
+    k: int = 80
+    num_workers: int = 12
+    u_grid: int = 1
+    v_grid: int = 1
+    x_grid: int = 1
+    y_grid: int = 1
+    num_iters: int = 30
+    gpu: int = 3
+    lambda_p: float = 0.05
+    lambda_q: float = 0.05
+    lrate: float = 0.0
+    alpha: float = 0.01
+    beta: float = 0.01
+    seed: int = 0
+    precision: str = "fp16"
+    lanes: int = 0
+    quiet: bool = True
+    epochs_per_launch: int = 0
+    verbose_epochs: bool = False
+
+    @property
+    def ux(self) -> int:
+        return self.u_grid * (1 if self.u_grid * self.v_grid == 1 else self.x_grid)
+
+    @property
+    def vy(self) -> int:
+        return self.v_grid * (1 if self.u_grid * self.v_grid == 1 else self.y_grid)
+
+    def to_c(self) -> _lib.Params:
+        p = _lib.Params()
+        _lib.check(_lib.load().cumf_default_params(C.byref(p)))
+        for f in ("k", "num_workers", "u_grid", "v_grid", "x_grid", "y_grid", "num_iters", "gpu",
+                  "lambda_p", "lambda_q", "lrate", "alpha", "beta", "seed", "lanes",
+                  "epochs_per_launch"):
+            setattr(p, f, getattr(self, f))
+        p.precision = PRECISIONS[self.precision] if isinstance(self.precision, str) else int(self.precision)
+        p.quiet = int(bool(self.quiet))
+        p.verbose_epochs = int(bool(self.verbose_epochs))
+        p.ux, p.vy = self.ux, self.vy
+        return p
+
+    @staticmethod
+    def from_c(p: _lib.Params) -> "Parameter":
+        inv = {v: k for k, v in PRECISIONS.items()}
+        return Parameter(k=p.k, num_workers=p.num_workers, u_grid=p.u_grid, v_grid=p.v_grid,
+                         x_grid=p.x_grid, y_grid=p.y_grid, num_iters=p.num_iters, gpu=p.gpu,
+                         lambda_p=p.lambda_p, lambda_q=p.lambda_q, lrate=p.lrate, alpha=p.alpha,
+                         beta=p.beta, seed=p.seed, precision=inv[p.precision], lanes=p.lanes,
+                         quiet=bool(p.quiet))
+
+
+@dataclasses.dataclass
+class Argument:
+    """Argument (singleGPU/sgd.h:48-77)."""
+    param: Parameter
+    tr_path: str
+    va_path: str
+    model_path: str
+
+
+def parse_argument(argv: Sequence[str]) -> Argument:
+    """parse_argument (singleGPU/main.cpp:33-227); argv[0] is the program name."""
+    lib = _lib.load()
+    arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+    out = _lib.Args()
+    rc = lib.cumf_parse_args(len(argv), arr, C.byref(out))
+    if rc != 0:
+        raise ValueError(lib.cumf_last_error().decode())
+    return Argument(Parameter.from_c(out.param), out.tr_path.decode(), out.va_path.decode(),
+                    out.model_path.decode())
+
+
+class MFProblem:
+    """mf_problem (singleGPU/sgd.h:85-108): m, n, nnz and the 12-byte records R."""
+
+    def __init__(self, c: _lib.Problem):
+        self._c = c
+
+    @staticmethod
+    def from_arrays(u, v, r, m: Optional[int] = None, n: Optional[int] = None,
+                    pinned: bool = False) -> "MFProblem":
+        u = np.asarray(u, dtype=np.int32)
+        v = np.asarray(v, dtype=np.int32)
+        r = np.asarray(r, dtype=np.float32)
+        nnz = len(u)
+        c = _lib.Problem()
+        _lib.check(_lib.load().cumf_alloc_problem(nnz, int(pinned), C.byref(c)))
+        prob = MFProblem(c)
+        rec = prob.records
+        rec["u"], rec["v"], rec["r"] = u, v, r
+        c.m = int(m) if m is not None else (int(u.max()) + 1 if nnz else 1)
+        c.n = int(n) if n is not None else (int(v.max()) + 1 if nnz else 1)
+        c.m, c.n = max(c.m, 1), max(c.n, 1)
+        return prob
+
+    @property
+    def m(self) -> int:
+        return self._c.m
+
+    @property
+    def n(self) -> int:
+        return self._c.n
+
+    @property
+    def nnz(self) -> int:
+        return self._c.nnz
+
+    @property
+    def records(self) -> np.ndarray:
+        """Zero-copy structured view (u, v, r) of the records."""
+        if self._c.nnz == 0:
+            return np.zeros(0, dtype=NODE_DTYPE)
+        buf = (C.c_char * (12 * self._c.nnz)).from_address(C.addressof(self._c.R.contents))
+        return np.frombuffer(buf, dtype=NODE_DTYPE)
+
+    def write(self, path: str) -> None:
+        _lib.check(_lib.load().cumf_write_problem(path.encode(), C.byref(self._c)))
+
+    def __del__(self):
+        try:
+            if self._c.R:
+                _lib.load().cumf_free_problem(C.byref(self._c))
+        except Exception:
+            pass
+
+
+def read_problem(path: str, pinned: bool = True) -> MFProblem:
+    """read_problem (singleGPU/sgd.cu:190-335)."""
+    c = _lib.Problem()
+    _lib.check(_lib.load().cumf_read_problem(path.encode(), int(pinned), C.byref(c)))
+    return MFProblem(c)
+
+
+class MFModel:
+    """mf_model as written to the model file: fp32 P (m x k), Q (n x k) and b."""
+
+    def __init__(self, c: _lib.Model):
+        self._c = c
+
+    @staticmethod
+    def from_arrays(P: np.ndarray, Q: np.ndarray, b: float) -> "MFModel":
+        P = np.ascontiguousarray(P, dtype=np.float32)
+        Q = np.ascontiguousarray(Q, dtype=np.float32)
+        c = _lib.Model()
+        _lib.check(_lib.load().cumf_alloc_model(P.shape[0], Q.shape[0], P.shape[1], C.byref(c)))
+        mod = MFModel(c)
+        mod.P[...] = P
+        mod.Q[...] = Q
+        c.b = b
+        return mod
+
+    def _view(self, ptr, rows: int) -> np.ndarray:
+        if rows * self._c.k == 0:
+            return np.zeros((rows, self._c.k), dtype=np.float32)
+        return np.ctypeslib.as_array(ptr, shape=(rows, self._c.k))
+
+    @property
+    def P(self) -> np.ndarray:
+        return self._view(self._c.P, self._c.m)
+
+    @property
+    def Q(self) -> np.ndarray:
+        return self._view(self._c.Q, self._c.n)
+
+    @property
+    def m(self) -> int:
+        return self._c.m
+
+    @property
+    def n(self) -> int:
+        return self._c.n
+
+    @property
+    def k(self) -> int:
+        return self._c.k
+
+    @property
+    def b(self) -> float:
+        return self._c.b
+
+    def __del__(self):
+        try:
+            if self._c.P or self._c.Q:
+                _lib.load().cumf_free_model(C.byref(self._c))
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class TrainStats:
+    prep_ms: float
+    train_ms: float
+    export_ms: float
+    total_ms: float
+    updates_per_sec: float
+    samples_per_epoch: int
+    mean: float
+    std_dev: float
+    mode: int
+    num_workers: int
+    lanes: int
+
+
+def sgd_train(tr: MFProblem, va: Optional[MFProblem], param: Parameter,
+              with_stats: bool = False):
+    """sgd_train (singleGPU/sgd.cu:638-690); `tr` is not modified."""
+    out = _lib.Model()
+    st = _lib.TrainStats()
+    p = param.to_c()
+    rc = _lib.load().cumf_train(C.byref(tr._c), C.byref(va._c) if va is not None else None,
+                                C.byref(p), C.byref(out), C.byref(st))
+    _lib.check(rc)
+    model = MFModel(out)
+    if with_stats:
+        stats = TrainStats(**{f: getattr(st, f) for f, _ in _lib.TrainStats._fields_ if f != "reserved_"})
+        return model, stats
+    return model
+
+
+def save_model(model: MFModel, path: str) -> None:
+    """save_model (singleGPU/main.cpp:231-273)."""
+    _lib.check(_lib.load().cumf_save_model(C.byref(model._c), path.encode()))
+
+
+def mf_load_model(path: str) -> MFModel:
+    """mf_load_model (test/mf.cpp:3706-3777)."""
+    c = _lib.Model()
+    _lib.check(_lib.load().cumf_load_model(path.encode(), C.byref(c)))
+    return MFModel(c)
+
+
+load_model = mf_load_model
+
+
+def calc_rmse(prob: MFProblem, model: MFModel) -> float:
+    """calc_rmse (test/mf.cpp:3815-3839), evaluated on the GPU."""
+    out = C.c_double()
+    _lib.check(_lib.load().cumf_rmse(C.byref(prob._c), C.byref(model._c), C.byref(out)))
+    return out.value
+
+
+def lr_schedule(alpha: float, beta: float, lrate: float, n: int) -> np.ndarray:
+    """Learning-rate table of singleGPU/sgd_kernel.cu:144-149."""
+    out = np.zeros(n, dtype=np.float32)
+    _lib.check(_lib.load().cumf_lr_schedule(alpha, beta, lrate, n,
+                                            out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def batches_per_worker(nnz: int, num_workers: int) -> int:
+    return int(_lib.load().cumf_batches_per_worker(nnz, num_workers))
+
+
+def random_map(seed: int, size: int) -> np.ndarray:
+    """gen_random_map (singleGPU/sgd.cu:39-53) for a given srand seed."""
+    out = np.zeros(size, dtype=np.int32)
+    _lib.check(_lib.load().cumf_random_map(seed & 0xffffffff, size,
+                                           out.ctypes.data_as(C.POINTER(C.c_int32))))
+    return out
+
+
+def grid_problem(records: np.ndarray, m: int, n: int, ux: int, vy: int):
+    """grid_problem (singleGPU/sgd.cu:411-487) in place on a structured record array;
+    returns (grid_size, u_seg, v_seg)."""
+    assert records.dtype == NODE_DTYPE and records.flags.c_contiguous
+    gs = np.zeros(ux * vy, dtype=np.int64)
+    us, vs = C.c_int64(), C.c_int64()
+    _lib.check(_lib.load().cumf_grid_problem(
+        records.ctypes.data_as(C.POINTER(_lib.Node)), len(records), m, n, ux, vy,
+        gs.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(us), C.byref(vs)))
+    return gs, us.value, vs.value
+
+
+def device_info(gpu: int = 0):
+    sm, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    _lib.check(_lib.load().cumf_device_info(gpu, C.byref(sm), C.byref(ma), C.byref(mi)))
+    return sm.value, ma.value, mi.value
+
+
+def default_workers(sm_count: int, k: int, precision: str = "fp16", lanes: int = 0) -> int:
+    return int(_lib.load().cumf_default_workers(sm_count, k, PRECISIONS[precision], lanes))
+
+
+# ---- device-level entry points (integer device addresses, e.g. torch.Tensor.data_ptr()) ----
+
+def sgd_update(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, precision: str,
+               num_workers: int, lanes: int, d_lr: int, first_epoch: int, n_epochs: int,
+               lambda_p: float, lambda_q: float, seed: int, d_status: int = 0,
+               stream: int = 0) -> None:
+    """Batch-Hogwild epochs on caller-owned device buffers (sgd_kernel.cu:212-248)."""
+    _lib.check(_lib.load().cumf_sgd_update(d_R, nnz, d_P, m, d_Q, n, k, PRECISIONS[precision],
+                                           num_workers, lanes, d_lr, first_epoch, n_epochs,
+                                           lambda_p, lambda_q, seed, d_status or None,
+                                           stream or None))
+
+
+def dev_init_factors(d: int, rows: int, k: int, precision: str, seed: int, tag: int,
+                     stream: int = 0) -> None:
+    _lib.check(_lib.load().cumf_dev_init_factors(d, rows, k, PRECISIONS[precision], seed, tag,
+                                                 stream or None))
+
+
+def dev_export_factors(d_in: int, precision: str, d_map: int, rows: int, k: int, factor: float,
+                       d_out: int, stream: int = 0) -> None:
+    _lib.check(_lib.load().cumf_dev_export_factors(d_in, PRECISIONS[precision], d_map or None,
+                                                   rows, k, factor, d_out, stream or None))
+
+
+def dev_shuffle_scale(d_in: int, d_out: int, nnz: int, d_pmap: int, m: int, d_qmap: int, n: int,
+                      scale: float, d_status: int = 0, stream: int = 0) -> None:
+    _lib.check(_lib.load().cumf_dev_shuffle_scale(d_in, d_out, nnz, d_pmap or None, m,
+                                                  d_qmap or None, n, scale, d_status or None,
+                                                  stream or None))
+
+
+def dev_rating_stats(d_R: int, nnz: int, stream: int = 0):
+    mean, std = C.c_double(), C.c_double()
+    _lib.check(_lib.load().cumf_dev_rating_stats(d_R, nnz, C.byref(mean), C.byref(std),
+                                                 stream or None))
+    return mean.value, std.value
+
+
+def dev_rmse(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, b: float,
+             stream: int = 0) -> float:
+    out = C.c_double()
+    _lib.check(_lib.load().cumf_dev_rmse(d_R, nnz, d_P, m, d_Q, n, k, b, C.byref(out),
+                                         stream or None))
+    return out.value

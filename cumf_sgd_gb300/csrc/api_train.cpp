@@ -1,0 +1,507 @@
+// api_train.cpp - sgd_train orchestration (modes A, B, C), the RMSE evaluator entry
+// points and the device-level wrappers of the C ABI.
+//
+// Mode A (u*v == 1, singleGPU/sgd_kernel.cu:212-248): the whole problem lives in HBM.  The
+// raw records are copied once; stats, id shuffle, scaling, factor init, the SGD epochs and
+// the fp32 export all run on the device, and only the final fp32 P and Q come back.
+// Modes B and C (u*v > 1) keep the ratings and factors in host memory and stream blocks
+// through the device (see stream_train below).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "cumf_sgd.h"
+#include "glibc_shuffle.h"
+#include "internal.h"
+
+namespace cumf {
+
+namespace {
+
+// RAII device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t alloc(size_t b) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = b;
+        return cudaMalloc(&p, b ? b : 16);
+    }
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct Stream {
+    cudaStream_t s = nullptr;
+    ~Stream() {
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+struct Event {
+    cudaEvent_t e = nullptr;
+    ~Event() {
+        if (e) cudaEventDestroy(e);
+    }
+    cudaError_t create() { return cudaEventCreate(&e); }
+};
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+bool valid_k(int k) { return k == 32 || k == 64 || k == 128 || k == 256; }
+
+int check_params(const cumf_params *p) {
+    if (!p) return fail(CUMF_ERR_ARG, "params is NULL");
+    if (!valid_k(p->k)) return fail(CUMF_ERR_ARG, "k must be 32, 64, 128 or 256 (got " + std::to_string(p->k) + ")");
+    if (p->num_workers < 1) return fail(CUMF_ERR_ARG, "num_workers must be positive");
+    if (p->num_iters < 0) return fail(CUMF_ERR_ARG, "num_iters must be >= 0");
+    if (p->u_grid < 1 || p->v_grid < 1 || p->x_grid < 1 || p->y_grid < 1)
+        return fail(CUMF_ERR_ARG, "grid sizes must be positive");
+    if (p->precision < CUMF_FP16 || p->precision > CUMF_FP16_SR) return fail(CUMF_ERR_ARG, "unknown precision");
+    if (p->lanes != 0 && !lanes_supported(p->k, p->precision, p->lanes))
+        return fail(CUMF_ERR_ARG, "unsupported lane count " + std::to_string(p->lanes) + " for k=" + std::to_string(p->k));
+    return CUMF_OK;
+}
+
+int select_device(int gpu) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return fail(CUMF_ERR_NODEVICE, "no CUDA device visible");
+    }
+    int dev = gpu % count;  // main.cpp:292-294
+    if (dev < 0) dev += count;
+    CUMF_CUDA(cudaSetDevice(dev));
+    return CUMF_OK;
+}
+
+// Host-side fp16/bf16 -> fp32 (exact widening), for the streamed modes' export.
+float half_bits_to_float(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    const uint32_t exp = (h >> 10) & 0x1f, man = h & 0x3ffu;
+    uint32_t bits;
+    if (exp == 0) {
+        if (man == 0) {
+            bits = sign;
+        } else {  // subnormal: renormalise
+            int e = -1;
+            uint32_t mm = man;
+            do {
+                mm <<= 1;
+                ++e;
+            } while ((mm & 0x400u) == 0);
+            bits = sign | ((uint32_t)(127 - 15 - e) << 23) | ((mm & 0x3ffu) << 13);
+        }
+    } else if (exp == 0x1f) {
+        bits = sign | 0x7f800000u | (man << 13);
+    } else {
+        bits = sign | ((exp + 127 - 15) << 23) | (man << 13);
+    }
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+float store_to_float(const void *base, int64_t idx, int precision) {
+    if (precision == CUMF_FP32) return reinterpret_cast<const float *>(base)[idx];
+    const uint16_t h = reinterpret_cast<const uint16_t *>(base)[idx];
+    if (precision == CUMF_BF16 || precision == CUMF_BF16_SR) {
+        const uint32_t bits = (uint32_t)h << 16;
+        float f;
+        memcpy(&f, &bits, 4);
+        return f;
+    }
+    return half_bits_to_float(h);
+}
+
+struct Prepared {
+    float ave = 0, std_dev = 0, scale = 1;
+    std::vector<int32_t> pmap, qmap;
+    GlibcRand rng{0};
+};
+
+// Rating statistics -> float mean/std and the scale max(1e-4, std) (sgd.cu:78-96, 648-649).
+void finish_stats(double sum, double sum2, int64_t nnz, Prepared &pr) {
+    double ex = nnz ? sum / (double)nnz : 0.0;
+    double ex2 = nnz ? sum2 / (double)nnz : 0.0;
+    pr.ave = (float)ex;
+    pr.std_dev = (float)sqrt(ex2 - ex * ex);
+    pr.scale = std::max(1e-4f, pr.std_dev);
+}
+
+// gen_random_map x2 (sgd.cu:656-657): both maps restart the glibc stream from the same seed
+// (srand(time(NULL)) is called inside each).  The stream continues after the q map into the
+// block shuffles of modes B/C (sgd_kernel.cu:263-267, 411-431).
+void make_maps(uint32_t seed, int32_t m, int32_t n, Prepared &pr) {
+    pr.pmap.resize(m);
+    pr.qmap.resize(n);
+    GlibcRand r1(seed);
+    for (int32_t i = 0; i < m; ++i) pr.pmap[i] = i;
+    glibc_random_shuffle(pr.pmap.data(), m, r1);
+    pr.rng.reseed(seed);
+    for (int32_t i = 0; i < n; ++i) pr.qmap[i] = i;
+    glibc_random_shuffle(pr.qmap.data(), n, pr.rng);
+}
+
+void print_args(const cumf_params &p) {
+    printf("k          :%d\n", p.k);
+    printf("num_workers:%d\n", p.num_workers);
+    printf("u_grid     :%d\n", p.u_grid);
+    printf("v_grid     :%d\n", p.v_grid);
+    printf("x_grid     :%d\n", p.x_grid);
+    printf("y_grid     :%d\n", p.y_grid);
+    printf("ux         :%d\n", p.ux);
+    printf("vy         :%d\n", p.vy);
+    printf("num_iters  :%d\n", p.num_iters);
+    printf("gpu        :%d\n", p.gpu);
+    printf("lambda_p   :%.5f\n", p.lambda_p);
+    printf("lambda_q   :%.5f\n", p.lambda_q);
+    printf("lrate      :%.5f\n", p.lrate);
+    printf("alpha      :%.4f\n", p.alpha);
+    printf("beta       :%.4f\n", p.beta);
+}
+
+// Per-epoch validation of the in-progress model against a raw test set on the device.
+struct EpochEval {
+    const cumf_problem *va = nullptr;
+    DevBuf d_va, d_pf, d_qf, d_part, d_sum;
+    int32_t m = 0, n = 0, k = 0;
+    int init(const cumf_problem *v, int32_t m_, int32_t n_, int k_, cudaStream_t s) {
+        va = v;
+        m = m_;
+        n = n_;
+        k = k_;
+        CUMF_CUDA(d_va.alloc(std::max<int64_t>(1, v->nnz) * sizeof(cumf_node)));
+        if (v->nnz) CUMF_CUDA(cudaMemcpyAsync(d_va.p, v->R, v->nnz * sizeof(cumf_node), cudaMemcpyHostToDevice, s));
+        CUMF_CUDA(d_pf.alloc((size_t)m * k * sizeof(float)));
+        CUMF_CUDA(d_qf.alloc((size_t)n * k * sizeof(float)));
+        CUMF_CUDA(d_part.alloc(rmse_blocks(v->nnz) * sizeof(double)));
+        CUMF_CUDA(d_sum.alloc(sizeof(double)));
+        return CUMF_OK;
+    }
+    // Exports the current factors exactly as the final model would be and evaluates.
+    int eval(const void *P, const void *Q, int precision, const int32_t *pmap,
+             const int32_t *qmap, float factor, float b, cudaStream_t s, double *rmse) {
+        CUMF_CUDA(launch_export(P, precision, pmap, m, k, factor, d_pf.as<float>(), s));
+        CUMF_CUDA(launch_export(Q, precision, qmap, n, k, factor, d_qf.as<float>(), s));
+        CUMF_CUDA(launch_rmse(d_va.as<cumf_node>(), va->nnz, d_pf.as<float>(), m, d_qf.as<float>(),
+                              n, k, b, d_part.as<double>(), d_sum.as<double>(), s));
+        double sum = 0;
+        CUMF_CUDA(cudaMemcpyAsync(&sum, d_sum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CUMF_CUDA(cudaStreamSynchronize(s));
+        *rmse = va->nnz ? sqrt(sum / (double)va->nnz) : 0.0;
+        return CUMF_OK;
+    }
+};
+
+int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_params &p,
+                 int workers, int lanes, cumf_model *out, cumf_train_stats *st) {
+    const double t0 = now_ms();
+    const int64_t nnz = tr->nnz;
+    const int32_t m = tr->m, n = tr->n;
+    const int k = p.k;
+    Stream stream;
+    CUMF_CUDA(cudaStreamCreateWithFlags(&stream.s, cudaStreamNonBlocking));
+    cudaStream_t s = stream.s;
+
+    DevBuf d_R, d_part, d_small, d_pmap, d_qmap, d_P, d_Q, d_lr, d_status, d_pf, d_qf;
+    CUMF_CUDA(d_R.alloc(std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
+    if (nnz) CUMF_CUDA(cudaMemcpyAsync(d_R.p, tr->R, nnz * sizeof(cumf_node), cudaMemcpyHostToDevice, s));
+
+    // collect_data on the device.
+    Prepared pr;
+    CUMF_CUDA(d_part.alloc(2 * stats_blocks(nnz) * sizeof(double)));
+    CUMF_CUDA(d_small.alloc(4 * sizeof(double)));
+    CUMF_CUDA(d_status.alloc(sizeof(int)));
+    CUMF_CUDA(cudaMemsetAsync(d_status.p, 0, sizeof(int), s));
+    CUMF_CUDA(launch_rating_stats(d_R.as<cumf_node>(), nnz, d_part.as<double>(), d_small.as<double>(), s));
+    double sums[2] = {0, 0};
+    CUMF_CUDA(cudaMemcpyAsync(sums, d_small.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+
+    // Id maps on the host (sequential glibc stream) while the stats run.
+    make_maps((uint32_t)p.seed, m, n, pr);
+    CUMF_CUDA(d_pmap.alloc((size_t)m * sizeof(int32_t)));
+    CUMF_CUDA(d_qmap.alloc((size_t)n * sizeof(int32_t)));
+    CUMF_CUDA(cudaMemcpyAsync(d_pmap.p, pr.pmap.data(), (size_t)m * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CUMF_CUDA(cudaMemcpyAsync(d_qmap.p, pr.qmap.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    finish_stats(sums[0], sums[1], nnz, pr);
+
+    // shuffle_problem + scale_problem in one pass: r * (float)(1.0/scale) (sgd.cu:672).
+    const float rscale = (float)(1.0 / pr.scale);
+    CUMF_CUDA(launch_shuffle_scale(d_R.as<cumf_node>(), d_R.as<cumf_node>(), nnz, d_pmap.as<int32_t>(), m,
+                                   d_qmap.as<int32_t>(), n, rscale, d_status.as<int>(), s));
+    const float lambda_p = p.lambda_p / pr.scale, lambda_q = p.lambda_q / pr.scale;  // sgd.cu:673-674
+
+    // init_model: every row, including rows without ratings (sgd.cu:548-591).
+    const int eb = elem_bytes(p.precision);
+    CUMF_CUDA(d_P.alloc((size_t)m * k * eb));
+    CUMF_CUDA(d_Q.alloc((size_t)n * k * eb));
+    CUMF_CUDA(launch_init_factors(d_P.p, m, k, p.precision, p.seed, 1, s));
+    CUMF_CUDA(launch_init_factors(d_Q.p, n, k, p.precision, p.seed, 2, s));
+
+    std::vector<float> lr(std::max(1, p.num_iters + 4));
+    cumf_lr_schedule(p.alpha, p.beta, p.lrate, (int)lr.size(), lr.data());
+    CUMF_CUDA(d_lr.alloc(lr.size() * sizeof(float)));
+    CUMF_CUDA(cudaMemcpyAsync(d_lr.p, lr.data(), lr.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+
+    const float factor = (float)sqrt(pr.scale);  // scale_model (sgd.cu:598)
+    const float b = pr.ave / pr.std_dev;           // model->b (sgd.cu:679)
+    EpochEval ev;
+    const bool per_epoch = p.verbose_epochs && va && va->nnz > 0;
+    if (per_epoch) {
+        if (int rc = ev.init(va, m, n, k, s)) return rc;
+    }
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    const double t1 = now_ms();
+
+    // SGD epochs.
+    Event e0, e1;
+    CUMF_CUDA(e0.create());
+    CUMF_CUDA(e1.create());
+    int lanes_used = lanes;
+    double train_ms = 0;
+    const int per_launch = per_epoch ? 1 : (p.epochs_per_launch > 0 ? p.epochs_per_launch : std::max(1, p.num_iters));
+    for (int ep = 0; ep < p.num_iters; ep += per_launch) {
+        const int cnt = std::min(per_launch, p.num_iters - ep);
+        CUMF_CUDA(cudaEventRecord(e0.e, s));
+        CUMF_CUDA(launch_sgd_update(d_R.as<cumf_node>(), nnz, d_P.p, m, d_Q.p, n, k, p.precision, workers, lanes,
+                                    d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
+                                    &lanes_used));
+        CUMF_CUDA(cudaEventRecord(e1.e, s));
+        CUMF_CUDA(cudaEventSynchronize(e1.e));
+        float ms = 0;
+        CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
+        train_ms += ms;
+        if (per_epoch) {
+            double rmse = 0;
+            if (int rc = ev.eval(d_P.p, d_Q.p, p.precision, d_pmap.as<int32_t>(), d_qmap.as<int32_t>(), factor, b, s, &rmse))
+                return rc;
+            printf("{\"epoch\": %d, \"train_ms\": %.3f, \"elapsed_ms\": %.3f, \"test_rmse\": %.6f}\n", ep + cnt, ms,
+                   train_ms, rmse);
+            fflush(stdout);
+        }
+    }
+    int status = 0;
+    CUMF_CUDA(cudaMemcpyAsync(&status, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    const double t2 = now_ms();
+
+    // Export: fp32, unscaled, un-permuted (transform_feature_vector + scale_model + shuffle_model).
+    CUMF_CUDA(d_pf.alloc((size_t)m * k * sizeof(float)));
+    CUMF_CUDA(d_qf.alloc((size_t)n * k * sizeof(float)));
+    CUMF_CUDA(launch_export(d_P.p, p.precision, d_pmap.as<int32_t>(), m, k, factor, d_pf.as<float>(), s));
+    CUMF_CUDA(launch_export(d_Q.p, p.precision, d_qmap.as<int32_t>(), n, k, factor, d_qf.as<float>(), s));
+    if (int rc = cumf_alloc_model(m, n, k, out)) return rc;
+    out->b = b;
+    cudaError_t ce = cudaMemcpyAsync(out->P, d_pf.p, (size_t)m * k * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out->Q, d_qf.p, (size_t)n * k * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) {
+        cumf_free_model(out);
+        return cuda_fail(ce, "model export");
+    }
+    if (status != 0) {
+        cumf_free_model(out);
+        return fail(CUMF_ERR_RANGE, "a rating index was outside the factor matrices");
+    }
+    const double t3 = now_ms();
+    if (st) {
+        st->prep_ms = t1 - t0;
+        st->train_ms = train_ms;
+        st->export_ms = t3 - t2;
+        st->total_ms = t3 - t0;
+        st->updates_per_sec = train_ms > 0 ? (double)nnz * p.num_iters / (train_ms * 1e-3) : 0.0;
+        st->samples_per_epoch = (int64_t)workers * batches_per_worker(nnz, workers) * 128;
+        st->mean = pr.ave;
+        st->std_dev = pr.std_dev;
+        st->mode = 0;
+        st->num_workers = workers;
+        st->lanes = lanes_used;
+    }
+    if (!p.quiet) {
+        printf("update_per_sec:%f\n", train_ms > 0 ? (double)nnz * p.num_iters / (train_ms * 1e-3) : 0.0);
+        fflush(stdout);
+    }
+    return CUMF_OK;
+}
+
+}  // namespace
+
+int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int lanes,
+                 cumf_model *out, cumf_train_stats *st);
+
+}  // namespace cumf
+
+using namespace cumf;
+
+extern "C" {
+
+int cumf_device_info(int gpu, int *sm_count, int *cc_major, int *cc_minor) {
+    if (int rc = select_device(gpu)) return rc;
+    int dev = 0;
+    CUMF_CUDA(cudaGetDevice(&dev));
+    if (sm_count) CUMF_CUDA(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev));
+    if (cc_major) CUMF_CUDA(cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, dev));
+    if (cc_minor) CUMF_CUDA(cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev));
+    return CUMF_OK;
+}
+
+int cumf_default_workers(int sm_count, int k, int precision, int lanes) {
+    if (lanes == 0) lanes = default_lanes(k, precision);
+    const int w = resident_workers(k, precision, lanes, sm_count);
+    cudaGetLastError();
+    return w > 0 ? w : 52 * sm_count;
+}
+
+int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params *params,
+               cumf_model *out, cumf_train_stats *stats) {
+    if (!tr || !out) return fail(CUMF_ERR_ARG, "train: problem and model must not be NULL");
+    if (tr->nnz < 0 || (tr->nnz > 0 && !tr->R) || tr->m < 1 || tr->n < 1)
+        return fail(CUMF_ERR_ARG, "train: malformed problem");
+    memset(out, 0, sizeof(*out));
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (int rc = check_params(params)) return rc;
+    cumf_params p = *params;
+    if (p.u_grid * p.v_grid == 1) p.x_grid = p.y_grid = 1;
+    p.ux = p.u_grid * p.x_grid;
+    p.vy = p.v_grid * p.y_grid;
+    if (int rc = select_device(p.gpu)) return rc;
+    const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    const int workers = p.num_workers;
+    if (!p.quiet) {
+        print_args(p);
+        fflush(stdout);
+    }
+    if (p.ux * p.vy == 1) return train_mode_a(tr, va, p, workers, lanes, out, stats);
+    return stream_train(tr, p, workers, lanes, out, stats);
+}
+
+int cumf_rmse(const cumf_problem *te, const cumf_model *model, double *out) {
+    if (!te || !model || !out) return fail(CUMF_ERR_ARG, "rmse: NULL argument");
+    if (te->nnz == 0) {  // calc_rmse returns 0 for an empty set (mf.cpp:3818-3819)
+        *out = 0;
+        return CUMF_OK;
+    }
+    if (!te->R || !model->P || !model->Q || model->k <= 0) return fail(CUMF_ERR_ARG, "rmse: malformed input");
+    if (int rc = select_device(0)) return rc;
+    Stream stream;
+    CUMF_CUDA(cudaStreamCreateWithFlags(&stream.s, cudaStreamNonBlocking));
+    DevBuf d_R, d_P, d_Q, d_part, d_sum;
+    const size_t pb = (size_t)model->m * model->k * sizeof(float), qb = (size_t)model->n * model->k * sizeof(float);
+    CUMF_CUDA(d_R.alloc(te->nnz * sizeof(cumf_node)));
+    CUMF_CUDA(d_P.alloc(pb));
+    CUMF_CUDA(d_Q.alloc(qb));
+    CUMF_CUDA(d_part.alloc(rmse_blocks(te->nnz) * sizeof(double)));
+    CUMF_CUDA(d_sum.alloc(sizeof(double)));
+    CUMF_CUDA(cudaMemcpyAsync(d_R.p, te->R, te->nnz * sizeof(cumf_node), cudaMemcpyHostToDevice, stream.s));
+    if (pb) CUMF_CUDA(cudaMemcpyAsync(d_P.p, model->P, pb, cudaMemcpyHostToDevice, stream.s));
+    if (qb) CUMF_CUDA(cudaMemcpyAsync(d_Q.p, model->Q, qb, cudaMemcpyHostToDevice, stream.s));
+    CUMF_CUDA(launch_rmse(d_R.as<cumf_node>(), te->nnz, d_P.as<float>(), model->m, d_Q.as<float>(), model->n,
+                          model->k, model->b, d_part.as<double>(), d_sum.as<double>(), stream.s));
+    double sum = 0;
+    CUMF_CUDA(cudaMemcpyAsync(&sum, d_sum.p, sizeof(double), cudaMemcpyDeviceToHost, stream.s));
+    CUMF_CUDA(cudaStreamSynchronize(stream.s));
+    *out = sqrt(sum / (double)te->nnz);
+    return CUMF_OK;
+}
+
+// ---- device-level wrappers ---------------------------------------------------------
+
+int cumf_dev_init_factors(void *d_factors, int64_t rows, int k, int precision, uint64_t seed,
+                          uint32_t tag, void *stream) {
+    if (rows < 0 || k <= 0 || (rows > 0 && !d_factors)) return fail(CUMF_ERR_ARG, "init_factors: bad arguments");
+    if (precision < CUMF_FP16 || precision > CUMF_FP16_SR) return fail(CUMF_ERR_ARG, "unknown precision");
+    CUMF_CUDA(launch_init_factors(d_factors, rows, k, precision, seed, tag, (cudaStream_t)stream));
+    return CUMF_OK;
+}
+
+int cumf_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, void *d_Q, int32_t n,
+                    int k, int precision, int num_workers, int lanes, const float *d_lr,
+                    int first_epoch, int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                    int *d_status, void *stream) {
+    if (nnz < 0 || num_workers < 1 || first_epoch < 0 || n_epochs < 0 || m < 1 || n < 1)
+        return fail(CUMF_ERR_ARG, "sgd_update: bad sizes");
+    if (nnz > 0 && (!d_R || !d_P || !d_Q || !d_lr)) return fail(CUMF_ERR_ARG, "sgd_update: NULL pointer");
+    if (!valid_k(k)) return fail(CUMF_ERR_ARG, "sgd_update: unsupported k " + std::to_string(k));
+    if (precision < CUMF_FP16 || precision > CUMF_FP16_SR) return fail(CUMF_ERR_ARG, "unknown precision");
+    if (lanes != 0 && !lanes_supported(k, precision, lanes)) return fail(CUMF_ERR_ARG, "unsupported lane count");
+    if (batches_per_worker(nnz, num_workers) * 4 > 0x7fffffffll)
+        return fail(CUMF_ERR_ARG, "sgd_update: too many batches per worker");
+    CUMF_CUDA(launch_sgd_update(d_R, nnz, d_P, m, d_Q, n, k, precision, num_workers, lanes, d_lr, first_epoch,
+                                n_epochs, lambda_p, lambda_q, seed, d_status, (cudaStream_t)stream, nullptr));
+    return CUMF_OK;
+}
+
+int cumf_dev_rating_stats(const cumf_node *d_R, int64_t nnz, double *mean, double *std_dev, void *stream) {
+    if (nnz < 0 || (nnz > 0 && !d_R) || !mean || !std_dev) return fail(CUMF_ERR_ARG, "rating_stats: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf part, sum;
+    CUMF_CUDA(part.alloc(2 * stats_blocks(nnz) * sizeof(double)));
+    CUMF_CUDA(sum.alloc(2 * sizeof(double)));
+    CUMF_CUDA(launch_rating_stats(d_R, nnz, part.as<double>(), sum.as<double>(), s));
+    double h[2];
+    CUMF_CUDA(cudaMemcpyAsync(h, sum.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    const double ex = nnz ? h[0] / nnz : 0.0, ex2 = nnz ? h[1] / nnz : 0.0;
+    *mean = ex;
+    *std_dev = sqrt(ex2 - ex * ex);
+    return CUMF_OK;
+}
+
+int cumf_dev_shuffle_scale(const cumf_node *d_in, cumf_node *d_out, int64_t nnz, const int32_t *d_p_map,
+                           int32_t m, const int32_t *d_q_map, int32_t n, float scale, int *d_status,
+                           void *stream) {
+    if (nnz < 0 || (nnz > 0 && (!d_in || !d_out))) return fail(CUMF_ERR_ARG, "shuffle_scale: bad arguments");
+    CUMF_CUDA(launch_shuffle_scale(d_in, d_out, nnz, d_p_map, m, d_q_map, n, scale, d_status, (cudaStream_t)stream));
+    return CUMF_OK;
+}
+
+int cumf_dev_export_factors(const void *d_in, int precision, const int32_t *d_map, int64_t rows, int k,
+                            float factor, float *d_out, void *stream) {
+    if (rows < 0 || k <= 0 || (rows > 0 && (!d_in || !d_out))) return fail(CUMF_ERR_ARG, "export: bad arguments");
+    if (precision < CUMF_FP16 || precision > CUMF_FP16_SR) return fail(CUMF_ERR_ARG, "unknown precision");
+    CUMF_CUDA(launch_export(d_in, precision, d_map, rows, k, factor, d_out, (cudaStream_t)stream));
+    return CUMF_OK;
+}
+
+int cumf_dev_rmse(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m, const float *d_Q, int32_t n,
+                  int k, float b, double *out_rmse, void *stream) {
+    if (nnz < 0 || k <= 0 || !out_rmse || (nnz > 0 && (!d_R || !d_P || !d_Q)))
+        return fail(CUMF_ERR_ARG, "dev_rmse: bad arguments");
+    if (nnz == 0) {
+        *out_rmse = 0;
+        return CUMF_OK;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf part, sum;
+    CUMF_CUDA(part.alloc(rmse_blocks(nnz) * sizeof(double)));
+    CUMF_CUDA(sum.alloc(sizeof(double)));
+    CUMF_CUDA(launch_rmse(d_R, nnz, d_P, m, d_Q, n, k, b, part.as<double>(), sum.as<double>(), s));
+    double h = 0;
+    CUMF_CUDA(cudaMemcpyAsync(&h, sum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    *out_rmse = sqrt(h / (double)nnz);
+    return CUMF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// internal.h - declarations shared by the library's translation units (not exported).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "cumf_sgd.h"
+
+namespace cumf {
+
+// ---- error reporting ---------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define CUMF_CUDA(call)                                   \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// ---- schedule helpers ----------------------------------------------------------------
+inline int64_t batches_per_worker(int64_t nnz, int workers) {
+    // ceil(nnz / (workers * 128)) as in sgd_kernel.cu:203 (computed in integers).
+    const int64_t per = (int64_t)workers * 128;
+    return (nnz + per - 1) / per;
+}
+
+// ---- sgd_update.cu -------------------------------------------------------------------
+int default_lanes(int k, int precision);
+bool lanes_supported(int k, int precision, int lanes);
+int workers_per_block(int lanes);
+int resident_workers(int k, int precision, int lanes, int sm_count);
+cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m,
+                              void *d_Q, int32_t n, int k, int precision, int num_workers,
+                              int lanes, const float *d_lr, int first_epoch, int n_epochs,
+                              float lambda_p, float lambda_q, uint64_t seed, int *d_status,
+                              cudaStream_t stream, int *lanes_used);
+
+// ---- prep.cu ---------------------------------------------------------------------------
+cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,
+                                uint32_t tag, cudaStream_t s);
+// Partial sums (sum r, sum r^2) per block into d_part[2*blocks]; returns blocks used.
+int stats_blocks(int64_t nnz);
+cudaError_t launch_rating_stats(const cumf_node *d_R, int64_t nnz, double *d_part,
+                                double *d_out2, cudaStream_t s);
+cudaError_t launch_shuffle_scale(const cumf_node *in, cumf_node *out, int64_t nnz,
+                                 const int32_t *pmap, int32_t m, const int32_t *qmap,
+                                 int32_t n, float scale, int *d_status, cudaStream_t s);
+cudaError_t launch_export(const void *in, int precision, const int32_t *map, int64_t rows,
+                          int k, float factor, float *out, cudaStream_t s);
+int rmse_blocks(int64_t nnz);
+cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
+                        const float *Q, int32_t n, int k, float b, double *d_part,
+                        double *d_sum, cudaStream_t s);
+
+// Size in bytes of one factor element for a precision.
+inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }
+
+}  // namespace cumf

@@ -1,0 +1,241 @@
+// prep.cu - data preparation, factor init, fp32 export and the RMSE evaluator.
+//
+// Reference counterparts:
+//   init_factors    random_init / init_feature      singleGPU/sgd.cu:497-546
+//   rating_stats    collect_data                    singleGPU/sgd.cu:78-96
+//   shuffle_scale   shuffle_problem + scale_problem singleGPU/sgd.cu:126-134, 98-124
+//   export          transform_half + scale_model + shuffle_model
+//                                                   singleGPU/sgd_kernel.cu:29-68,
+//                                                   singleGPU/sgd.cu:593-635
+//   rmse            calc_rmse / mf_predict          test/mf.cpp:3794-3839
+// All are HBM-streaming kernels (grid-stride, coalesced); the reductions are two-pass with a
+// fixed grid so results do not depend on scheduling.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace cumf {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kReduceBlocks = 1024;  // fixed grid of the two-pass reductions
+
+template <int KIND>
+__global__ void init_kernel(void *out, uint64_t count, int k, uint64_t key) {
+    using S = Scalar<KIND>;
+    typename S::T *o = reinterpret_cast<typename S::T *>(out);
+    // (float)sqrt(1.0/k), the reference's scale (sgd.cu:519).
+    const float scale = (float)sqrt(1.0 / (double)k);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        o[i] = S::from_float(__fmul_rn(init_uniform(key, i), scale));
+    }
+}
+
+__device__ __forceinline__ double block_sum(double x, double *sh) {
+    for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = x;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+__global__ void stats_kernel(const cumf_node *R, uint64_t nnz, double *part) {
+    __shared__ double sh[2][kThreads / 32];
+    double s = 0.0, s2 = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nnz;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const double r = (double)R[i].r;
+        s += r;
+        s2 += r * r;
+    }
+    const double a = block_sum(s, sh[0]);
+    const double b = block_sum(s2, sh[1]);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+
+// Sums `count` pairs of partials in index order (deterministic).
+__global__ void sum_pairs_kernel(const double *part, int count, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < count; ++i) {
+            a += part[2 * i];
+            b += part[2 * i + 1];
+        }
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
+__global__ void shuffle_scale_kernel(const cumf_node *in, cumf_node *out, uint64_t nnz,
+                                     const int32_t *pmap, uint32_t m, const int32_t *qmap,
+                                     uint32_t n, float scale, int *status) {
+    int bad = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nnz;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        cumf_node x = in[i];
+        const uint32_t u = (uint32_t)x.u, v = (uint32_t)x.v;
+        if (u < m && v < n) {
+            x.u = pmap ? pmap[u] : x.u;
+            x.v = qmap ? qmap[v] : x.v;
+        } else {
+            bad = 1;
+        }
+        x.r = __fmul_rn(x.r, scale);
+        out[i] = x;
+    }
+    if (bad && status) atomicExch(status, (int)CUMF_ERR_RANGE);
+}
+
+template <int KIND>
+__global__ void export_kernel(const void *in, const int32_t *map, uint64_t rows, int k,
+                              float factor, float *out) {
+    using S = Scalar<KIND>;
+    const typename S::T *src = reinterpret_cast<const typename S::T *>(in);
+    const uint64_t count = rows * (uint64_t)k;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t o = i / (uint64_t)k, j = i - o * (uint64_t)k;
+        const uint64_t srow = map ? (uint64_t)(uint32_t)map[o] : o;
+        out[i] = __fmul_rn(S::to_float(src[srow * (uint64_t)k + j]), factor);
+    }
+}
+
+// Eight lanes per rating; float dot in fp32, squared error rounded to fp32 and summed in
+// fp64 as calc_rmse does (`mf_float e = r - z; loss += e*e;`, mf.cpp:3831-3834).
+constexpr int kRmseLanes = 8;
+
+__global__ void rmse_kernel(const cumf_node *R, uint64_t nnz, const float *P, uint32_t m,
+                            const float *Q, uint32_t n, int k, float b, double *part) {
+    __shared__ double sh[kThreads / 32];
+    const int lane = threadIdx.x % kRmseLanes;
+    const uint64_t group = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kRmseLanes;
+    const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / kRmseLanes;
+    const unsigned gmask = 0xffu << ((threadIdx.x & 31) & ~(kRmseLanes - 1));
+    double acc = 0.0;
+    for (uint64_t i = group; i < nnz; i += groups) {
+        const cumf_node x = R[i];
+        const uint32_t u = (uint32_t)x.u, v = (uint32_t)x.v;
+        float z;
+        if (u < m && v < n) {
+            const float *p = P + (uint64_t)u * k;
+            const float *q = Q + (uint64_t)v * k;
+            float s = 0.f;
+            if ((k & 3) == 0) {
+                const float4 *p4 = reinterpret_cast<const float4 *>(p);
+                const float4 *q4 = reinterpret_cast<const float4 *>(q);
+                for (int c = lane; c < (k >> 2); c += kRmseLanes) {
+                    const float4 a = __ldg(p4 + c), bq = __ldg(q4 + c);
+                    s = __fmaf_rn(a.x, bq.x, s);
+                    s = __fmaf_rn(a.y, bq.y, s);
+                    s = __fmaf_rn(a.z, bq.z, s);
+                    s = __fmaf_rn(a.w, bq.w, s);
+                }
+            } else {
+                for (int c = lane; c < k; c += kRmseLanes) s = __fmaf_rn(__ldg(p + c), __ldg(q + c), s);
+            }
+            for (int o = kRmseLanes / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+            z = isnan(s) ? b : s;
+        } else {
+            z = b;
+        }
+        if (lane == 0) {
+            const float e = x.r - z;
+            acc += (double)__fmul_rn(e, e);
+        }
+    }
+    const double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void sum_kernel(const double *part, int count, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double a = 0.0;
+        for (int i = 0; i < count; ++i) a += part[i];
+        out[0] = a;
+    }
+}
+
+int grid_for(uint64_t items, int per_thread = 1) {
+    uint64_t blocks = (items + (uint64_t)kThreads * per_thread - 1) / ((uint64_t)kThreads * per_thread);
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152ull * 32) blocks = 152ull * 32;
+    return (int)blocks;
+}
+
+}  // namespace
+
+cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,
+                                uint32_t tag, cudaStream_t s) {
+    const uint64_t count = (uint64_t)rows * (uint64_t)k;
+    if (count == 0) return cudaSuccess;
+    const uint64_t key = init_key(seed, tag);
+    const int g = grid_for(count, 4);
+    switch (store_of_precision(precision)) {
+        case kHalf: init_kernel<kHalf><<<g, kThreads, 0, s>>>(d, count, k, key); break;
+        case kBf16: init_kernel<kBf16><<<g, kThreads, 0, s>>>(d, count, k, key); break;
+        default: init_kernel<kFloat><<<g, kThreads, 0, s>>>(d, count, k, key); break;
+    }
+    return cudaGetLastError();
+}
+
+int stats_blocks(int64_t nnz) {
+    (void)nnz;
+    return kReduceBlocks;
+}
+
+cudaError_t launch_rating_stats(const cumf_node *d_R, int64_t nnz, double *d_part,
+                                double *d_out2, cudaStream_t s) {
+    stats_kernel<<<kReduceBlocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, d_part);
+    sum_pairs_kernel<<<1, 32, 0, s>>>(d_part, kReduceBlocks, d_out2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shuffle_scale(const cumf_node *in, cumf_node *out, int64_t nnz,
+                                 const int32_t *pmap, int32_t m, const int32_t *qmap,
+                                 int32_t n, float scale, int *d_status, cudaStream_t s) {
+    if (nnz <= 0) return cudaSuccess;
+    shuffle_scale_kernel<<<grid_for((uint64_t)nnz, 4), kThreads, 0, s>>>(
+        in, out, (uint64_t)nnz, pmap, (uint32_t)m, qmap, (uint32_t)n, scale, d_status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export(const void *in, int precision, const int32_t *map, int64_t rows,
+                          int k, float factor, float *out, cudaStream_t s) {
+    const uint64_t count = (uint64_t)rows * (uint64_t)k;
+    if (count == 0) return cudaSuccess;
+    const int g = grid_for(count, 4);
+    switch (store_of_precision(precision)) {
+        case kHalf: export_kernel<kHalf><<<g, kThreads, 0, s>>>(in, map, rows, k, factor, out); break;
+        case kBf16: export_kernel<kBf16><<<g, kThreads, 0, s>>>(in, map, rows, k, factor, out); break;
+        default: export_kernel<kFloat><<<g, kThreads, 0, s>>>(in, map, rows, k, factor, out); break;
+    }
+    return cudaGetLastError();
+}
+
+int rmse_blocks(int64_t nnz) {
+    (void)nnz;
+    return kReduceBlocks;
+}
+
+cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
+                        const float *Q, int32_t n, int k, float b, double *d_part,
+                        double *d_sum, cudaStream_t s) {
+    rmse_kernel<<<kReduceBlocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, P, (uint32_t)m, Q,
+                                                   (uint32_t)n, k, b, d_part);
+    sum_kernel<<<1, 32, 0, s>>>(d_part, kReduceBlocks, d_sum);
+    return cudaGetLastError();
+}
+
+}  // namespace cumf

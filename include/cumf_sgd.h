@@ -1,0 +1,255 @@
+/*
+ * cumf_sgd.h - C ABI of the GB300-native batch-Hogwild SGD matrix-factorization path.
+ *
+ * Drop-in boundary for cuMF_SGD's single-GPU trainer.  Every entry point replaces one
+ * reference interface (cited per declaration as file:line inside the cuMF_SGD project):
+ *
+ *   singleGPU/sgd.h:140        mf_problem read_problem(string)           -> cumf_read_problem
+ *   singleGPU/sgd.h:141        mf_model* sgd_train(mf_problem*, ...)      -> cumf_train
+ *   singleGPU/sgd_kernel.h:17  sgd_update_k128(Parameter, ...)            -> cumf_sgd_update
+ *   singleGPU/main.cpp:231     save_model(mf_model const*, char const*)   -> cumf_save_model
+ *   singleGPU/main.cpp:33      parse_argument(int, char**)                -> cumf_parse_args
+ *   test/mf.cpp:3706           mf_load_model(char const*)                 -> cumf_load_model
+ *   test/mf.cpp:3815           calc_rmse(mf_problem*, mf_model*)          -> cumf_rmse
+ *
+ * Conventions (differences from the reference are deliberate and listed here):
+ *   - every call returns an int status (CUMF_OK == 0); nothing calls exit().  The message of
+ *     the last failure on the calling thread is returned by cumf_last_error().
+ *   - inputs are const: cumf_train copies the ratings and permutes/scales the copy (the
+ *     reference mutates the caller's problem in place, sgd.cu:661,672).
+ *   - no global RNG state: every random choice is a pure function of params.seed
+ *     (the reference seeds from time(NULL) and clock(), sgd.cu:42,494).
+ *   - device pointers in the cumf_dev_* / cumf_sgd_update family are plain addresses of
+ *     device memory owned by the caller; `stream` is a cudaStream_t passed as void*.
+ * Plain C types only; no C++ or torch types cross this boundary.
+ */
+#ifndef CUMF_SGD_H_
+#define CUMF_SGD_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUMF_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------- */
+enum {
+    CUMF_OK = 0,
+    CUMF_ERR_ARG = 1,      /* invalid argument / unsupported parameter                  */
+    CUMF_ERR_IO = 2,       /* file missing, unreadable, short, or unwritable            */
+    CUMF_ERR_FORMAT = 3,   /* malformed rating or model file (negative id, bad header)  */
+    CUMF_ERR_CUDA = 4,     /* a CUDA runtime call failed                                */
+    CUMF_ERR_NOMEM = 5,    /* host or device allocation failed                          */
+    CUMF_ERR_RANGE = 6,    /* a rating index lies outside [0,m) x [0,n)                 */
+    CUMF_ERR_TIMEOUT = 7,  /* a bounded device-side wait gave up                        */
+    CUMF_ERR_NODEVICE = 8  /* no CUDA device visible                                    */
+};
+
+/* ---- factor storage precision (update arithmetic is always fp32) ------------------ */
+enum {
+    CUMF_FP16 = 0,     /* reference: half storage, round-to-nearest (warp32.h:89-99)    */
+    CUMF_BF16 = 1,     /* bf16 storage, round-to-nearest                                 */
+    CUMF_FP32 = 2,     /* fp32 storage                                                   */
+    CUMF_BF16_SR = 3,  /* bf16 storage, stochastic rounding on every factor write        */
+    CUMF_FP16_SR = 4   /* fp16 storage, stochastic rounding on every factor write        */
+};
+
+/* ---- records ---------------------------------------------------------------------- */
+/* One rating: the 12-byte on-disk record {int32 u, int32 v, float32 r}.
+ * Same layout as mf_node (singleGPU/sgd.h:79-83) and the file format (sgd.cu:251-253). */
+typedef struct cumf_node {
+    int32_t u;
+    int32_t v;
+    float r;
+} cumf_node;
+
+/* mf_problem (singleGPU/sgd.h:85-108), host side.  m = max u + 1, n = max v + 1, each at
+ * least 1 (sgd.cu:202-203,256-257).  R is page-locked when `pinned` is 1. */
+typedef struct cumf_problem {
+    int32_t m;
+    int32_t n;
+    int64_t nnz;
+    cumf_node *R;
+    int32_t pinned;
+    int32_t reserved_;
+} cumf_problem;
+
+/* Parameter (singleGPU/sgd.h:26-46) plus the build's additions.  cumf_default_params
+ * fills the reference defaults (sgd.h:45). */
+typedef struct cumf_params {
+    int32_t k;             /* factor length; 32, 64, 128 or 256 (reference: 128 only)  */
+    int32_t num_workers;   /* -s: Hogwild workers; rounded up to a multiple of 4         */
+    int32_t u_grid, v_grid, x_grid, y_grid;   /* -u -v -x -y                            */
+    int32_t ux, vy;        /* u_grid*x_grid, v_grid*y_grid (main.cpp:224-225)           */
+    int32_t num_iters;     /* -t                                                        */
+    int32_t gpu;           /* -g: device id, taken modulo the device count              */
+    float lambda_p, lambda_q;  /* -l p[,q]                                              */
+    float lrate;           /* -r: additive learning-rate floor (sgd_kernel.cu:146)      */
+    float alpha, beta;     /* -a -b: lr(t) = alpha/(1+beta*t^1.5) + lrate               */
+    /* additions ---------------------------------------------------------------------- */
+    uint64_t seed;         /* seeds the id shuffle, factor init and sample draws        */
+    int32_t precision;     /* CUMF_FP16 ...                                              */
+    int32_t lanes;         /* lanes cooperating on one rating: 0 = auto, else 4..32     */
+    int32_t quiet;         /* 1 = no informational stdout                               */
+    int32_t epochs_per_launch; /* mode A: 0 = one launch for all epochs (reference)     */
+    int32_t verbose_epochs;    /* 1 = print one JSON line per epoch (needs a test set)  */
+    int32_t reserved_[5];
+} cumf_params;
+
+/* mf_model (singleGPU/sgd.h:110-138) as the model file holds it (main.cpp:247-266):
+ * P is m x k and Q is n x k, row-major fp32, already unscaled and un-permuted. */
+typedef struct cumf_model {
+    int32_t fun;
+    int32_t m;
+    int32_t n;
+    int32_t k;
+    float b;
+    int32_t pinned;        /* 1 if P and Q are page-locked (set by the allocator)       */
+    float *P;
+    float *Q;
+} cumf_model;
+
+/* Timings and counters of one cumf_train call (the reference prints update_per_sec from
+ * clock(), sgd_kernel.cu:243-244; these are wall/CUDA-event times). */
+typedef struct cumf_train_stats {
+    double prep_ms;        /* H2D + stats + shuffle + scale + init                      */
+    double train_ms;       /* SGD epochs only (CUDA events)                             */
+    double export_ms;      /* fp16->fp32, unscale, un-permute, D2H                      */
+    double total_ms;
+    double updates_per_sec;/* nnz * num_iters / train time (reference convention)       */
+    int64_t samples_per_epoch; /* workers * batches * 128                               */
+    float mean, std_dev;   /* rating statistics (sgd.cu:78-96)                         */
+    int32_t mode;          /* 0 = A (in HBM), 1 = B (u x v), 2 = C (x x y streaming)    */
+    int32_t num_workers;
+    int32_t lanes;
+    int32_t reserved_[5];
+} cumf_train_stats;
+
+/* CLI arguments: Argument (singleGPU/sgd.h:48-77). */
+typedef struct cumf_args {
+    cumf_params param;
+    char tr_path[1024];
+    char va_path[1024];
+    char model_path[1024];
+} cumf_args;
+
+/* ---- library ---------------------------------------------------------------------- */
+int cumf_abi_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char *cumf_last_error(void);
+/* Reference defaults (singleGPU/sgd.h:45) plus seed 0, FP16, auto lanes. */
+int cumf_default_params(cumf_params *p);
+/* parse_argument (singleGPU/main.cpp:33-227): same flags, same -s rounding, the same
+ * default model path (<basename of train file>.model), u*v==1 forces x=y=1.  Long flags
+ * added: --seed N, --precision fp16|bf16|fp32|bf16sr|fp16sr, --lanes N, --quiet.
+ * Returns CUMF_ERR_ARG with the reference's message on bad input. */
+int cumf_parse_args(int argc, char **argv, cumf_args *out);
+
+/* ---- host I/O --------------------------------------------------------------------- */
+/* read_problem (singleGPU/sgd.cu:190-335): single file, or shards path0..path79 read in
+ * parallel when path0 exists.  nnz = size/12 (a trailing partial record is ignored, as in
+ * the reference).  Negative ids are rejected (CUMF_ERR_FORMAT).  pinned=1 allocates R
+ * page-locked (the reference always does, sgd.cu:240). */
+int cumf_read_problem(const char *path, int pinned, cumf_problem *out);
+/* Writes nnz 12-byte records (the inverse of read_problem; data/netflix/transform.cpp:37-42). */
+int cumf_write_problem(const char *path, const cumf_problem *prob);
+/* Allocates an empty problem of nnz records (pinned if asked). */
+int cumf_alloc_problem(int64_t nnz, int pinned, cumf_problem *out);
+int cumf_free_problem(cumf_problem *prob);
+
+/* save_model (singleGPU/main.cpp:231-273): i32 fun=0, i32 m, i32 n, i32 k, f32 b, then
+ * m*k f32 P, then n*k f32 Q.  Fails with CUMF_ERR_IO if the path cannot be written
+ * (the reference prints and carries on with a NULL FILE*, main.cpp:242-245). */
+int cumf_save_model(const cumf_model *model, const char *path);
+/* mf_load_model (test/mf.cpp:3706-3777); also checks the file length. */
+int cumf_load_model(const char *path, cumf_model *out);
+int cumf_alloc_model(int32_t m, int32_t n, int32_t k, cumf_model *out);
+int cumf_free_model(cumf_model *model);
+
+/* ---- training --------------------------------------------------------------------- */
+/* sgd_train (singleGPU/sgd.cu:638-690): stats -> shuffle ids -> grid -> scale -> init ->
+ * batch-Hogwild epochs -> fp32 export, unscale, un-permute.  `va` may be NULL; when given,
+ * and params.verbose_epochs is 1, the test RMSE is printed after each epoch.  `out` is
+ * allocated by the call (free with cumf_free_model); `stats` may be NULL. */
+int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params *params,
+               cumf_model *out, cumf_train_stats *stats);
+
+/* calc_rmse (test/mf.cpp:3815-3839) on the GPU: sqrt(sum (r - <p_u,q_v>)^2 / nnz) with the
+ * squared error rounded to fp32 and summed in fp64; ids outside the model or a NaN dot
+ * predict model->b (mf.cpp:3794-3813). */
+int cumf_rmse(const cumf_problem *te, const cumf_model *model, double *out);
+
+/* ---- device-level entry points (caller-owned device memory) ----------------------- */
+/* The learning-rate table lr[t] = (float)(alpha/(1+beta*t^1.5) + lrate), t < n
+ * (singleGPU/sgd_kernel.cu:144-149), written to host memory. */
+int cumf_lr_schedule(float alpha, float beta, float lrate, int n, float *out);
+/* Per-worker batch budget ceil(nnz/(workers*128)) (singleGPU/sgd_kernel.cu:203). */
+int64_t cumf_batches_per_worker(int64_t nnz, int num_workers);
+
+/* random_init / init_feature (singleGPU/sgd.cu:497-546): every element of a rows x k
+ * factor matrix is U(0,1] * (float)sqrt(1/k), rounded to the storage type.  The uniform
+ * is a pure function of (seed, tag, element index). */
+int cumf_dev_init_factors(void *d_factors, int64_t rows, int k, int precision,
+                          uint64_t seed, uint32_t tag, void *stream);
+
+/* sgd_update_k128 mode A / sgd_k128_kernel_hogwild_warp32_lrate
+ * (singleGPU/sgd_kernel.cu:212-248, singleGPU/sgd_k128_kernel_hogwild_warp32.h:3-104):
+ * runs epochs [first_epoch, first_epoch + n_epochs) of batch-Hogwild SGD in place on
+ * d_P (m x k) and d_Q (n x k) over d_R (nnz records, ids already in range, ratings
+ * scaled).  Each of `num_workers` workers does ceil(nnz/(num_workers*128)) batches per
+ * epoch; a batch is 128 consecutive records from a uniformly drawn start (wrapping).
+ * d_lr holds at least first_epoch+n_epochs learning rates (device memory).
+ * d_status (device int, may be NULL) receives CUMF_ERR_RANGE if an index is out of range
+ * (such a rating is skipped).  lanes = 0 picks the tuned default. */
+int cumf_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, void *d_Q,
+                    int32_t n, int k, int precision, int num_workers, int lanes,
+                    const float *d_lr, int first_epoch, int n_epochs, float lambda_p,
+                    float lambda_q, uint64_t seed, int *d_status, void *stream);
+
+/* collect_data (singleGPU/sgd.cu:78-96) on the device: mean and population std of the
+ * ratings, accumulated in fp64.  Results are written to host doubles. */
+int cumf_dev_rating_stats(const cumf_node *d_R, int64_t nnz, double *mean, double *std_dev,
+                          void *stream);
+
+/* shuffle_problem + scale_problem (singleGPU/sgd.cu:126-134, 98-124, at u=v=1):
+ * out[i] = {p_map[u], q_map[v], r * scale}; flags CUMF_ERR_RANGE in d_status when an id is
+ * outside [0,m) x [0,n).  In-place (d_out == d_in) is allowed. */
+int cumf_dev_shuffle_scale(const cumf_node *d_in, cumf_node *d_out, int64_t nnz,
+                           const int32_t *d_p_map, int32_t m, const int32_t *d_q_map,
+                           int32_t n, float scale, int *d_status, void *stream);
+
+/* transform_half + scale_model + shuffle_model (singleGPU/sgd_kernel.cu:29-68,
+ * sgd.cu:593-635): out[o] = float(in[map[o]]) * factor for every row o < rows (map may be
+ * NULL for identity). */
+int cumf_dev_export_factors(const void *d_in, int precision, const int32_t *d_map,
+                            int64_t rows, int k, float factor, float *d_out, void *stream);
+
+/* calc_rmse (test/mf.cpp:3815-3839) over device data: fp32 model P (m x k), Q (n x k).
+ * The squared-error sum is reduced deterministically; *out_rmse is a host double. */
+int cumf_dev_rmse(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m,
+                  const float *d_Q, int32_t n, int k, float b, double *out_rmse,
+                  void *stream);
+
+/* Device SM count and the default worker count (52 warps-worth of workers per SM,
+ * README.md:61, scaled for the lane width in use). */
+int cumf_device_info(int gpu, int *sm_count, int *cc_major, int *cc_minor);
+int cumf_default_workers(int sm_count, int k, int precision, int lanes);
+
+/* glibc-compatible id shuffle used for bit-exact layout parity: fills map[0..size) with
+ * the permutation that srand(seed); random_shuffle(identity) produces
+ * (singleGPU/sgd.cu:39-53), without touching the process-wide rand() state. */
+int cumf_random_map(uint32_t seed, int32_t size, int32_t *map);
+
+/* grid_problem (singleGPU/sgd.cu:411-487): buckets R in place into ux*vy blocks in the
+ * reference's exact order; grid_size receives ux*vy counts, u_seg/v_seg the segment sizes. */
+int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, int vy,
+                      int64_t *grid_size, int64_t *u_seg, int64_t *v_seg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUMF_SGD_H_ */

@@ -1,0 +1,247 @@
+"""GPU kernels against the oracle, through the C ABI.  Tolerances are written per test:
+integer / layout / init / export work is bit-exact; one-worker SGD is bit-exact against the
+oracle replaying this kernel's dot order, and within 1e-5 (relative to max |P|, |Q|) of the
+oracle replaying the reference kernel's order (warp32.h:62-83); Hogwild test RMSE is within
+0.002 of the serial oracle after the same epochs."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import cumf_sgd_gb300 as cm
+from cumf_sgd_gb300 import _lib, synth
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["fp32", "fp16", "bf16", "bf16sr", "fp16sr"]
+
+
+def tt():
+    import torch
+    return torch
+
+
+def dev(a, cuda):
+    torch = tt()
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(cuda)
+
+
+def small_problem(m, n, nnz, seed, lo=1, hi=5):
+    rng = np.random.default_rng(seed)
+    rec = np.empty(nnz, dtype=cm.NODE_DTYPE)
+    rec["u"] = rng.integers(0, m, nnz)
+    rec["v"] = rng.integers(0, n, nnz)
+    rec["r"] = rng.integers(lo, hi + 1, nnz).astype(np.float32)
+    return rec
+
+
+def storage_to_float(t, precision, rows, k):
+    torch = tt()
+    if precision == "fp32":
+        return t.view(torch.float32).reshape(rows, k).float().cpu().numpy()
+    dt = torch.float16 if precision in ("fp16", "fp16sr") else torch.bfloat16
+    return t.view(dt).reshape(rows, k).float().cpu().numpy()
+
+
+def elem(precision):
+    return 4 if precision == "fp32" else 2
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("k", [32, 128, 256])
+def test_init_factors_bit_exact(lib, orc, cuda, precision, k):
+    torch = tt()
+    rows = 333
+    buf = torch.empty(rows * k * elem(precision), dtype=torch.uint8, device=cuda)
+    cm.dev_init_factors(buf.data_ptr(), rows, k, precision, seed=77, tag=1)
+    torch.cuda.synchronize()
+    got = storage_to_float(buf, precision, rows, k)
+    np.testing.assert_array_equal(got, orc.init_factors(rows, k, precision, 77, 1))
+    assert got.min() > 0 and got.max() <= np.float32(1 / np.sqrt(k)) * 1.001
+
+
+def run_gpu_epochs(cuda, rec, m, n, k, precision, workers, lanes, lr, epochs, lp, lq, seed):
+    torch = tt()
+    d_R = dev(rec, cuda)
+    P = torch.empty(m * k * elem(precision), dtype=torch.uint8, device=cuda)
+    Q = torch.empty(n * k * elem(precision), dtype=torch.uint8, device=cuda)
+    cm.dev_init_factors(P.data_ptr(), m, k, precision, seed, 1)
+    cm.dev_init_factors(Q.data_ptr(), n, k, precision, seed, 2)
+    d_lr = torch.from_numpy(lr).to(cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    cm.sgd_update(d_R.data_ptr(), len(rec), P.data_ptr(), m, Q.data_ptr(), n, k, precision, workers, lanes,
+                  d_lr.data_ptr(), 0, epochs, lp, lq, seed, status.data_ptr())
+    torch.cuda.synchronize()
+    return storage_to_float(P, precision, m, k), storage_to_float(Q, precision, n, k), int(status.item())
+
+
+@pytest.mark.parametrize("precision", PRECS)
+@pytest.mark.parametrize("k,lanes", [(128, 0), (128, 8), (64, 0), (32, 0), (256, 0)])
+def test_single_worker_sgd_bit_exact(lib, orc, cuda, precision, k, lanes):
+    if precision == "fp32" and lanes == 8:
+        lanes = 16
+    m, n, nnz = 70, 45, 3000
+    rec = small_problem(m, n, nnz, 11)
+    rec["r"] = rec["r"] / np.float32(1.1)
+    lr = orc.lr_table(0.08, 0.3, 0.0, 8)
+    Pg, Qg, st = run_gpu_epochs(cuda, rec, m, n, k, precision, 1, lanes, lr, 3, 0.05, 0.04, 5)
+    assert st == 0
+    lanes_used = lanes or default_lanes(k, precision)
+    P = orc.init_factors(m, k, precision, 5, 1)
+    Q = orc.init_factors(n, k, precision, 5, 2)
+    skipped = orc.sgd_epochs(rec, P, Q, precision, 1, lr, 0, 3, 0.05, 0.04, 5, lanes=lanes_used)
+    assert skipped == 0
+    np.testing.assert_array_equal(Pg, P)
+    np.testing.assert_array_equal(Qg, Q)
+
+
+def default_lanes(k, precision):
+    # first listed kernel per (k, storage): one 16-byte word per lane, capped at 32 lanes
+    eb = 4 if precision == "fp32" else 2
+    return min(32, k * eb // 16)
+
+
+def test_single_worker_fp32_close_to_reference_order(lib, orc, cuda):
+    m, n, nnz, k = 80, 50, 4000, 128
+    rec = small_problem(m, n, nnz, 12)
+    lr = orc.lr_table(0.08, 0.3, 0.0, 8)
+    Pg, Qg, _ = run_gpu_epochs(cuda, rec, m, n, k, "fp32", 1, 0, lr, 4, 0.05, 0.05, 9)
+    P = orc.init_factors(m, k, "fp32", 9, 1)
+    Q = orc.init_factors(n, k, "fp32", 9, 2)
+    orc.sgd_epochs(rec, P, Q, "fp32", 1, lr, 0, 4, 0.05, 0.05, 9, dot_order=orc.OR_DOT_REF)
+    # tolerance: 1e-5 relative to the largest factor magnitude
+    assert np.abs(Pg - P).max() <= 1e-5 * np.abs(P).max()
+    assert np.abs(Qg - Q).max() <= 1e-5 * np.abs(Q).max()
+
+
+@pytest.mark.parametrize("nnz", [1, 7, 100, 127, 128, 129, 300])
+def test_wraparound_small_nnz_bit_exact(lib, orc, cuda, nnz):
+    m, n, k = 9, 6, 32
+    rec = small_problem(m, n, nnz, nnz)
+    lr = orc.lr_table(0.08, 0.3, 0.0, 8)
+    for workers in (1, 3):
+        Pg, Qg, _ = run_gpu_epochs(cuda, rec, m, n, k, "fp32", workers, 0, lr, 2, 0.05, 0.05, 3)
+        if workers == 1:
+            P = orc.init_factors(m, k, "fp32", 3, 1)
+            Q = orc.init_factors(n, k, "fp32", 3, 2)
+            orc.sgd_epochs(rec, P, Q, "fp32", 1, lr, 0, 2, 0.05, 0.05, 3, lanes=8)
+            np.testing.assert_array_equal(Pg, P)
+            np.testing.assert_array_equal(Qg, Q)
+        assert np.isfinite(Pg).all() and np.isfinite(Qg).all()
+
+
+def test_out_of_range_ids_are_flagged_and_skipped(lib, orc, cuda):
+    m, n, k = 20, 10, 64
+    rec = small_problem(m, n, 500, 4)
+    rec["u"][17] = m + 3
+    rec["v"][200] = -1
+    lr = orc.lr_table(0.08, 0.3, 0.0, 4)
+    Pg, Qg, st = run_gpu_epochs(cuda, rec, m, n, k, "fp32", 1, 0, lr, 1, 0.05, 0.05, 1)
+    assert st == _lib.CUMF_ERR_RANGE
+    P = orc.init_factors(m, k, "fp32", 1, 1)
+    Q = orc.init_factors(n, k, "fp32", 1, 2)
+    skipped = orc.sgd_epochs(rec, P, Q, "fp32", 1, lr, 0, 1, 0.05, 0.05, 1, lanes=16)
+    assert skipped > 0
+    np.testing.assert_array_equal(Pg, P)
+    np.testing.assert_array_equal(Qg, Q)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16sr"])
+def test_full_train_single_worker_matches_oracle(lib, orc, cuda, precision):
+    rec = small_problem(150, 90, 6000, 21)
+    prob = cm.MFProblem.from_arrays(rec["u"], rec["v"], rec["r"])
+    par = cm.Parameter(k=128, num_workers=1, num_iters=3, alpha=0.08, beta=0.3, seed=1234, gpu=0,
+                       precision=precision)
+    model, st = cm.sgd_train(prob, None, par, with_stats=True)
+    P, Q, b, ave, std = orc.train(rec, prob.m, prob.n, k=128, precision=precision, num_workers=1, num_iters=3,
+                                  alpha=0.08, beta=0.3, seed=1234, lanes=16)
+    assert np.float32(st.mean) == np.float32(ave) and np.float32(st.std_dev) == np.float32(std)
+    assert np.float32(model.b) == np.float32(b)
+    np.testing.assert_array_equal(model.P, P)
+    np.testing.assert_array_equal(model.Q, Q)
+    # and the input problem was not modified
+    assert prob.records.tobytes() == rec.tobytes()
+
+
+def test_gpu_rmse_matches_reference_golden(lib, cuda):
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "rmse.npz"))
+    i = 0
+    while f"rmse{i}" in g:
+        te = g[f"te{i}"]
+        prob = cm.MFProblem.from_arrays(te["u"], te["v"], te["r"])
+        model = cm.MFModel.from_arrays(g[f"P{i}"], g[f"Q{i}"], float(g[f"b{i}"]))
+        got = cm.calc_rmse(prob, model)
+        ref = float(g[f"rmse{i}"])
+        assert abs(got - ref) <= 1e-6 * ref, (i, got, ref)  # fp32 dot order differs; 1e-6 relative
+        i += 1
+
+
+def test_device_stats_shuffle_export_bit_exact(lib, orc, cuda):
+    torch = tt()
+    rec = small_problem(300, 200, 20000, 8)
+    rec["r"] += np.float32(0.37)
+    d = dev(rec, cuda)
+    mean, std = cm.dev_rating_stats(d.data_ptr(), len(rec))
+    a, s = orc.collect_data(rec)
+    assert np.float32(mean) == np.float32(a) and np.float32(std) == np.float32(s)
+    pm, qm = orc.gen_random_map(5, 300), orc.gen_random_map(5, 200)
+    dp, dq = torch.from_numpy(pm).to(cuda), torch.from_numpy(qm).to(cuda)
+    out = torch.empty_like(d)
+    sc = np.float32(1.0 / float(s))
+    cm.dev_shuffle_scale(d.data_ptr(), out.data_ptr(), len(rec), dp.data_ptr(), 300, dq.data_ptr(), 200, float(sc))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(cm.NODE_DTYPE)
+    exp = rec.copy()
+    exp["u"], exp["v"], exp["r"] = pm[rec["u"]], qm[rec["v"]], rec["r"] * sc
+    assert got.tobytes() == exp.tobytes()
+    for precision in ("fp16", "bf16", "fp32"):
+        k = 64
+        buf = torch.empty(300 * k * elem(precision), dtype=torch.uint8, device=cuda)
+        cm.dev_init_factors(buf.data_ptr(), 300, k, precision, 3, 1)
+        fo = torch.empty(300 * k, dtype=torch.float32, device=cuda)
+        f = np.float32(np.sqrt(np.float32(1.7)))
+        cm.dev_export_factors(buf.data_ptr(), precision, dp.data_ptr(), 300, k, float(f), fo.data_ptr())
+        torch.cuda.synchronize()
+        src = orc.init_factors(300, k, precision, 3, 1)
+        np.testing.assert_array_equal(fo.cpu().numpy().reshape(300, k), src[pm] * f)
+
+
+def test_hogwild_c1_rmse_within_0002_of_serial_oracle(lib, orc, cuda):
+    tr, te = synth.generate_c1(seed=1, device="cpu")
+    prob = cm.MFProblem.from_arrays(tr["u"], tr["v"], tr["r"], m=10000, n=2000)
+    test = cm.MFProblem.from_arrays(te["u"], te["v"], te["r"])
+    sm, _, _ = cm.device_info(0)
+    workers = cm.default_workers(sm, 128, "fp16")
+    par = cm.Parameter(k=128, num_workers=workers, num_iters=20, lambda_p=0.05, lambda_q=0.05, alpha=0.08,
+                       beta=0.3, seed=3, gpu=0, precision="fp16")
+    model = cm.sgd_train(prob, None, par)
+    gpu_rmse = cm.calc_rmse(test, model)
+    P, Q, b, _, _ = orc.train(tr, 10000, 2000, k=128, precision="fp16", num_workers=workers, num_iters=20,
+                              alpha=0.08, beta=0.3, seed=3, lanes=16)
+    cpu_rmse = orc.calc_rmse(te, P, Q, b)
+    assert abs(gpu_rmse - cpu_rmse) <= 0.002, (gpu_rmse, cpu_rmse)
+    assert gpu_rmse < 1.0
+
+
+def test_cli_train_and_predict(lib, orc, cuda, tmp_path):
+    rec = small_problem(400, 150, 30000, 31)
+    te = small_problem(400, 150, 3000, 32)
+    trp, tep, mp = str(tmp_path / "tr.bin"), str(tmp_path / "te.bin"), str(tmp_path / "tr.model")
+    rec.tofile(trp)
+    te.tofile(tep)
+    exe = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_sgd")
+    res = subprocess.run([exe, "-g", "0", "-l", "0.05", "-a", "0.08", "-b", "0.3", "-s", "64", "-k", "128",
+                          "-t", "5", "--seed", "2", "-p", tep, trp, mp], capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "update_per_sec:" in res.stdout and '"epoch": 5' in res.stdout
+    assert os.path.getsize(mp) == 20 + 4 * 128 * (400 + 150)
+    res = subprocess.run([os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_predict"), "-e", "0", tep, mp],
+                         capture_output=True, text=True)
+    assert res.returncode == 0
+    got = float(res.stdout.strip().split("=")[1])
+    m = cm.mf_load_model(mp)
+    assert abs(got - orc.calc_rmse(te, m.P, m.Q, m.b)) < 1e-4
