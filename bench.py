@@ -181,7 +181,7 @@ def _has_cuda():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp16")
@@ -189,6 +189,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--e2e-epochs", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the c2 size (tests only)")
     args = ap.parse_args()
@@ -232,14 +233,16 @@ def main():
     Q = torch.empty(n * K * eb, dtype=torch.uint8, device=dev)
     cm.dev_init_factors(P.data_ptr(), m, K, prec, rank, 1, sp)
     cm.dev_init_factors(Q.data_ptr(), n, K, prec, rank, 2, sp)
+    # Step s runs epoch s mod 20 of the 20-epoch job's learning-rate schedule.
+    job_epochs = 20
     epochs_total = args.warmup + args.steps
-    lr = torch.from_numpy(cm.lr_schedule(0.08, 0.3, 0.0, epochs_total + 4)).to(dev)
+    lr = torch.from_numpy(cm.lr_schedule(0.08, 0.3, 0.0, job_epochs + 4)).to(dev)
     lp = float(np.float32(0.05) / scale)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
 
     def epoch(e):
         cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m, Q.data_ptr(), n, K, prec, workers, args.lanes,
-                      lr.data_ptr(), e, 1, lp, lp, rank, status.data_ptr(), sp)
+                      lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp)
 
     for e in range(args.warmup):
         epoch(e)
@@ -276,7 +279,7 @@ def main():
 
     # End to end through the C ABI: pinned host ratings -> cumf_train (20 epochs) -> fp32 model.
     e2e = None
-    if True:
+    if not args.no_e2e:
         prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=m, n=n, pinned=True)
         tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
         par = cm.Parameter(k=K, num_workers=workers, num_iters=args.e2e_epochs, lambda_p=0.05, lambda_q=0.05,

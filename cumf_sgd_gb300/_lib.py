@@ -44,7 +44,13 @@ class Params(C.Structure):
                 ("alpha", C.c_float), ("beta", C.c_float),
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("lanes", C.c_int32),
                 ("quiet", C.c_int32), ("epochs_per_launch", C.c_int32),
-                ("verbose_epochs", C.c_int32), ("reserved_", C.c_int32 * 5)]
+                ("verbose_epochs", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
+                ("reserved_", C.c_int32 * 3)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
+                ("reserved_", C.c_int32 * 5)]
 
 
 class Model(C.Structure):
@@ -90,6 +96,9 @@ _SIGS = {
     "cumf_sgd_update": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32, C.c_int, C.c_int,
                                   C.c_int, C.c_int, _VP, C.c_int, C.c_int, C.c_float, C.c_float,
                                   C.c_uint64, _VP, _VP]),
+    "cumf_sgd_update_tuned": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32, C.c_int, C.c_int,
+                                        C.c_int, C.POINTER(Tuning), _VP, C.c_int, C.c_int, C.c_float,
+                                        C.c_float, C.c_uint64, _VP, _VP]),
     "cumf_dev_rating_stats": (C.c_int, [_VP, C.c_int64, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), _VP]),
     "cumf_dev_shuffle_scale": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32,

@@ -89,6 +89,8 @@ int cumf_default_params(cumf_params *p) {
     p->quiet = 0;
     p->epochs_per_launch = 0;
     p->verbose_epochs = 0;
+    p->prefetch = -1;
+    p->l2_hints = -1;
     return CUMF_OK;
 }
 

@@ -285,7 +285,11 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     for (int ep = 0; ep < p.num_iters; ep += per_launch) {
         const int cnt = std::min(per_launch, p.num_iters - ep);
         CUMF_CUDA(cudaEventRecord(e0.e, s));
-        CUMF_CUDA(launch_sgd_update(d_R.as<cumf_node>(), nnz, d_P.p, m, d_Q.p, n, k, p.precision, workers, lanes,
+        Tuning tu;
+        tu.lanes = lanes;
+        tu.prefetch = p.prefetch;
+        tu.hints = p.l2_hints;
+        CUMF_CUDA(launch_sgd_update(d_R.as<cumf_node>(), nnz, d_P.p, m, d_Q.p, n, k, p.precision, workers, tu,
                                     d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
                                     &lanes_used));
         CUMF_CUDA(cudaEventRecord(e1.e, s));
@@ -439,6 +443,26 @@ int cumf_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, voi
                     int k, int precision, int num_workers, int lanes, const float *d_lr,
                     int first_epoch, int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
                     int *d_status, void *stream) {
+    cumf_tuning t;
+    memset(&t, 0, sizeof(t));
+    t.lanes = lanes;
+    t.prefetch = -1;
+    t.l2_hints = -1;
+    return cumf_sgd_update_tuned(d_R, nnz, d_P, m, d_Q, n, k, precision, num_workers, &t, d_lr, first_epoch,
+                                 n_epochs, lambda_p, lambda_q, seed, d_status, stream);
+}
+
+int cumf_sgd_update_tuned(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, void *d_Q, int32_t n,
+                          int k, int precision, int num_workers, const cumf_tuning *tuning, const float *d_lr,
+                          int first_epoch, int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                          int *d_status, void *stream) {
+    Tuning tu;
+    if (tuning) {
+        tu.lanes = tuning->lanes;
+        tu.prefetch = tuning->prefetch;
+        tu.hints = tuning->l2_hints;
+    }
+    const int lanes = tu.lanes;
     if (nnz < 0 || num_workers < 1 || first_epoch < 0 || n_epochs < 0 || m < 1 || n < 1)
         return fail(CUMF_ERR_ARG, "sgd_update: bad sizes");
     if (nnz > 0 && (!d_R || !d_P || !d_Q || !d_lr)) return fail(CUMF_ERR_ARG, "sgd_update: NULL pointer");
@@ -447,7 +471,7 @@ int cumf_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, voi
     if (lanes != 0 && !lanes_supported(k, precision, lanes)) return fail(CUMF_ERR_ARG, "unsupported lane count");
     if (batches_per_worker(nnz, num_workers) * 4 > 0x7fffffffll)
         return fail(CUMF_ERR_ARG, "sgd_update: too many batches per worker");
-    CUMF_CUDA(launch_sgd_update(d_R, nnz, d_P, m, d_Q, n, k, precision, num_workers, lanes, d_lr, first_epoch,
+    CUMF_CUDA(launch_sgd_update(d_R, nnz, d_P, m, d_Q, n, k, precision, num_workers, tu, d_lr, first_epoch,
                                 n_epochs, lambda_p, lambda_q, seed, d_status, (cudaStream_t)stream, nullptr));
     return CUMF_OK;
 }

@@ -119,7 +119,38 @@ struct Scalar<kFloat> {
 
 // Cache-hinted 16-byte accesses.  Factor rows are read through L2 only (ld.global.cg):
 // other SMs write them concurrently (Hogwild), and a stale L1 copy would hide those writes.
+// `pol` is an L2 cache policy from createpolicy (evict_last keeps the factor working set
+// resident while the ratings stream past with evict_first).
 __device__ __forceinline__ uint4 ld_row(const uint4 *p) { return __ldcg(p); }
 __device__ __forceinline__ void st_row(uint4 *p, uint4 v) { __stcg(p, v); }
+
+__device__ __forceinline__ uint64_t l2_policy(bool hint, bool keep) {
+    uint64_t pol;
+    if (!hint)
+        asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;\n" : "=l"(pol));
+    else if (keep)
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(pol));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ uint4 ld_row_hint(const uint4 *p, uint64_t pol) {
+    uint4 v;
+    asm volatile("ld.global.cg.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;\n"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st_row_hint(uint4 *p, uint4 v, uint64_t pol) {
+    asm volatile("st.global.cg.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;\n" ::"l"(p), "r"(v.x),
+                 "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
+                 : "memory");
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2::evict_last [%0];\n" ::"l"(p));
+}
 
 }  // namespace cumf

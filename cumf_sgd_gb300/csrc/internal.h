@@ -28,15 +28,21 @@ inline int64_t batches_per_worker(int64_t nnz, int workers) {
 }
 
 // ---- sgd_update.cu -------------------------------------------------------------------
+struct Tuning {
+    int lanes = 0;      // 0 = default
+    int prefetch = -1;  // -1 = default
+    int hints = -1;     // -1 = default
+};
+Tuning resolve_tuning(int k, int precision, Tuning t);
 int default_lanes(int k, int precision);
 bool lanes_supported(int k, int precision, int lanes);
 int workers_per_block(int lanes);
 int resident_workers(int k, int precision, int lanes, int sm_count);
 cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m,
                               void *d_Q, int32_t n, int k, int precision, int num_workers,
-                              int lanes, const float *d_lr, int first_epoch, int n_epochs,
-                              float lambda_p, float lambda_q, uint64_t seed, int *d_status,
-                              cudaStream_t stream, int *lanes_used);
+                              const Tuning &tuning, const float *d_lr, int first_epoch,
+                              int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                              int *d_status, cudaStream_t stream, int *lanes_used);
 
 // ---- prep.cu ---------------------------------------------------------------------------
 cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,

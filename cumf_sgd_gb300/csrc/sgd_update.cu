@@ -30,6 +30,8 @@ namespace {
 
 constexpr int kBlock = 256;   // threads per block
 constexpr int kMinBlocks = 4; // >= 1024 resident threads per SM (<= 64 registers)
+constexpr int kDefaultPrefetch = 2;
+constexpr int kDefaultHints = 1;
 constexpr int kBatch = 128;   // records per batch (update_vector_size, sgd_kernel.cu:198)
 // Records staged in shared memory at a time: 32, or 16 for narrow groups (keeps the
 // staging buffer of a 256-thread block under 27 KB).
@@ -48,6 +50,8 @@ struct UpdateArgs {
     float lambda_p, lambda_q;
     uint64_t seed;
     int *status;
+    int prefetch;   // rows of record j+prefetch are pulled into L2 while record j runs (0 = off)
+    int hints;      // 1 = L2 eviction hints (ratings evict_first, factor rows evict_last)
 };
 
 // Copy of a word the compiler cannot see through: the update phase re-widens the packed
@@ -57,9 +61,10 @@ __device__ __forceinline__ uint4 opaque(uint4 w) {
     return w;
 }
 
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, uint64_t pol) {
     const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "l"(pol)
+                 : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
@@ -94,6 +99,11 @@ sgd_hogwild_kernel(const UpdateArgs a) {
     const uint64_t nnz = a.nnz;
     const float lp = a.lambda_p, lq = a.lambda_q;
     const int chunks = a.batches * CPB;
+    const int pd = a.prefetch;
+    const uint64_t pol_rec = l2_policy(a.hints != 0, false);
+    const uint64_t pol_row = l2_policy(a.hints != 0, true);
+    // Lanes whose 16-byte slice starts a 128-byte line issue the L2 prefetches.
+    const bool pf_lane = ((lane * NV * 16) & 127) == 0;
     int bad = 0;
 
     for (int ep = a.first_epoch; ep < a.first_epoch + a.n_epochs; ++ep) {
@@ -110,7 +120,7 @@ sgd_hogwild_kernel(const UpdateArgs a) {
                 const int word = lane + i * G;
                 uint64_t rec = base + (uint64_t)(word / 3);
                 while (rec >= nnz) rec -= nnz;
-                cp_async4(&s_rec[gib][buf][word % 3][word / 3], Rw + rec * 3 + (word % 3));
+                cp_async4(&s_rec[gib][buf][word % 3][word / 3], Rw + rec * 3 + (word % 3), pol_rec);
             }
             cp_async_commit();
         };
@@ -125,8 +135,8 @@ sgd_hogwild_kernel(const UpdateArgs a) {
         uint4 fp[NV], fq[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            fp[i] = ok ? ld_row(P + (uint64_t)u * ROW_WORDS + i) : make_uint4(0, 0, 0, 0);
-            fq[i] = ok ? ld_row(Q + (uint64_t)v * ROW_WORDS + i) : make_uint4(0, 0, 0, 0);
+            fp[i] = ok ? ld_row_hint(P + (uint64_t)u * ROW_WORDS + i, pol_row) : make_uint4(0, 0, 0, 0);
+            fq[i] = ok ? ld_row_hint(Q + (uint64_t)v * ROW_WORDS + i, pol_row) : make_uint4(0, 0, 0, 0);
         }
 
         for (int t = 0; t < chunks; ++t) {
@@ -136,6 +146,26 @@ sgd_hogwild_kernel(const UpdateArgs a) {
 
 #pragma unroll 1
             for (int j = 0; j < kChunk; ++j) {
+                // L2 prefetch of the rows of record j + pd (same or next chunk).
+                if (pd > 0) {
+                    const int jj = j + pd;
+                    uint32_t pu = 0xffffffffu, pv = 0xffffffffu;
+                    if (jj < kChunk) {
+                        pu = s_rec[gib][buf][0][jj];
+                        pv = s_rec[gib][buf][1][jj];
+                    } else if (has_next_chunk && jj - kChunk < kChunk) {
+                        if (jj == kChunk) {  // first look into the next chunk: wait for its copy
+                            cp_async_wait_all();
+                            __syncwarp(gmask);
+                        }
+                        pu = s_rec[gib][buf ^ 1][0][jj - kChunk];
+                        pv = s_rec[gib][buf ^ 1][1][jj - kChunk];
+                    }
+                    if (pf_lane && pu < a.m && pv < a.n) {
+                        prefetch_l2(P + (uint64_t)pu * ROW_WORDS);
+                        prefetch_l2(Q + (uint64_t)pv * ROW_WORDS);
+                    }
+                }
                 // Next record: same chunk, or the first record of the next chunk.
                 uint32_t un = 0xffffffffu, vn = 0xffffffffu;
                 if (j + 1 < kChunk) {
@@ -151,8 +181,8 @@ sgd_hogwild_kernel(const UpdateArgs a) {
                 uint4 np[NV], nq[NV];
 #pragma unroll
                 for (int i = 0; i < NV; ++i) {
-                    np[i] = okn ? ld_row(P + (uint64_t)un * ROW_WORDS + i) : make_uint4(0, 0, 0, 0);
-                    nq[i] = okn ? ld_row(Q + (uint64_t)vn * ROW_WORDS + i) : make_uint4(0, 0, 0, 0);
+                    np[i] = okn ? ld_row_hint(P + (uint64_t)un * ROW_WORDS + i, pol_row) : make_uint4(0, 0, 0, 0);
+                    nq[i] = okn ? ld_row_hint(Q + (uint64_t)vn * ROW_WORDS + i, pol_row) : make_uint4(0, 0, 0, 0);
                 }
 
                 if (ok) {
@@ -201,8 +231,8 @@ sgd_hogwild_kernel(const UpdateArgs a) {
                     }
 #pragma unroll
                     for (int i = 0; i < NV; ++i) {
-                        st_row(P + (uint64_t)u * ROW_WORDS + i, wp[i]);
-                        st_row(Q + (uint64_t)v * ROW_WORDS + i, wq[i]);
+                        st_row_hint(P + (uint64_t)u * ROW_WORDS + i, wp[i], pol_row);
+                        st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
                     }
                     // Forward the fresh rows when the next record reuses them (its loads
                     // were issued before these stores).
@@ -308,12 +338,21 @@ int resident_workers(int k, int precision, int lanes, int sm_count) {
     return blocks * sm_count * (kBlock / e->lanes);
 }
 
+Tuning resolve_tuning(int k, int precision, Tuning t) {
+    if (t.lanes == 0) t.lanes = default_lanes(k, precision);
+    if (t.prefetch < 0) t.prefetch = kDefaultPrefetch;
+    if (t.prefetch > 15) t.prefetch = 15;
+    if (t.hints < 0) t.hints = kDefaultHints;
+    return t;
+}
+
 cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m,
                               void *d_Q, int32_t n, int k, int precision, int num_workers,
-                              int lanes, const float *d_lr, int first_epoch, int n_epochs,
-                              float lambda_p, float lambda_q, uint64_t seed, int *d_status,
-                              cudaStream_t stream, int *lanes_used) {
-    const KernelEntry *e = find_kernel(k, precision, lanes);
+                              const Tuning &tuning, const float *d_lr, int first_epoch,
+                              int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                              int *d_status, cudaStream_t stream, int *lanes_used) {
+    const Tuning t = resolve_tuning(k, precision, tuning);
+    const KernelEntry *e = find_kernel(k, precision, t.lanes);
     if (!e) return cudaErrorInvalidValue;
     if (lanes_used) *lanes_used = e->lanes;
     if (nnz <= 0 || n_epochs <= 0 || num_workers <= 0) return cudaSuccess;
@@ -333,6 +372,8 @@ cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int3
     a.lambda_q = lambda_q;
     a.seed = seed;
     a.status = d_status;
+    a.prefetch = t.prefetch;
+    a.hints = t.hints;
     const int gpb = kBlock / e->lanes;
     const int blocks = (num_workers + gpb - 1) / gpb;
     e->fn<<<blocks, kBlock, 0, stream>>>(a);

@@ -96,8 +96,20 @@ typedef struct cumf_params {
     int32_t quiet;         /* 1 = no informational stdout                               */
     int32_t epochs_per_launch; /* mode A: 0 = one launch for all epochs (reference)     */
     int32_t verbose_epochs;    /* 1 = print one JSON line per epoch (needs a test set)  */
-    int32_t reserved_[5];
+    int32_t prefetch;      /* L2 prefetch distance in records: -1 = tuned default, 0 = off */
+    int32_t l2_hints;      /* L2 eviction hints: -1 = tuned default, 0 = off, 1 = on      */
+    int32_t reserved_[3];
 } cumf_params;
+
+/* Launch tuning of the update kernel (the knobs the autotuner searches). */
+typedef struct cumf_tuning {
+    int32_t lanes;         /* lanes per rating: 0 = default for (k, precision)           */
+    int32_t prefetch;      /* rows of record j+prefetch are pulled into L2 during record j;
+                              -1 = default, 0 = off, at most 15                          */
+    int32_t l2_hints;      /* -1 = default, 0 = none, 1 = ratings evict_first and factor
+                              rows evict_last                                            */
+    int32_t reserved_[5];
+} cumf_tuning;
 
 /* mf_model (singleGPU/sgd.h:110-138) as the model file holds it (main.cpp:247-266):
  * P is m x k and Q is n x k, row-major fp32, already unscaled and un-permuted. */
@@ -208,6 +220,13 @@ int cumf_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, voi
                     int32_t n, int k, int precision, int num_workers, int lanes,
                     const float *d_lr, int first_epoch, int n_epochs, float lambda_p,
                     float lambda_q, uint64_t seed, int *d_status, void *stream);
+
+/* cumf_sgd_update with explicit launch tuning (tuning may be NULL for the defaults). */
+int cumf_sgd_update_tuned(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t m, void *d_Q,
+                          int32_t n, int k, int precision, int num_workers,
+                          const cumf_tuning *tuning, const float *d_lr, int first_epoch,
+                          int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                          int *d_status, void *stream);
 
 /* collect_data (singleGPU/sgd.cu:78-96) on the device: mean and population std of the
  * ratings, accumulated in fp64.  Results are written to host doubles. */

@@ -157,7 +157,7 @@ def test_full_train_single_worker_matches_oracle(lib, orc, cuda, precision):
                        precision=precision)
     model, st = cm.sgd_train(prob, None, par, with_stats=True)
     P, Q, b, ave, std = orc.train(rec, prob.m, prob.n, k=128, precision=precision, num_workers=1, num_iters=3,
-                                  alpha=0.08, beta=0.3, seed=1234, lanes=16)
+                                  alpha=0.08, beta=0.3, seed=1234, lanes=default_lanes(128, precision))
     assert np.float32(st.mean) == np.float32(ave) and np.float32(st.std_dev) == np.float32(std)
     assert np.float32(model.b) == np.float32(b)
     np.testing.assert_array_equal(model.P, P)
