@@ -106,6 +106,8 @@ _SIGS = {
     "cumf_dev_export_factors": (C.c_int, [_VP, C.c_int, _VP, C.c_int64, C.c_int, C.c_float, _VP, _VP]),
     "cumf_dev_rmse": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32, C.c_int, C.c_float,
                                 C.POINTER(C.c_double), _VP]),
+    "cumf_dev_rmse_noalloc": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32, C.c_int, C.c_float,
+                                        C.POINTER(C.c_double), _VP]),
     "cumf_device_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cumf_default_workers": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "cumf_random_map": (C.c_int, [C.c_uint32, C.c_int32, C.POINTER(C.c_int32)]),

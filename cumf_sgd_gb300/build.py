@@ -30,6 +30,7 @@ LIB_SOURCES = [
     "api_io.cpp",
     "api_train.cpp",
     "stream_train.cpp",
+    "noalloc.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp"}
 

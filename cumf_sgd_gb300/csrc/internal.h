@@ -60,6 +60,10 @@ int rmse_blocks(int64_t nnz);
 cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
                         const float *Q, int32_t n, int k, float b, double *d_part,
                         double *d_sum, cudaStream_t s);
+// The same evaluator on a caller-chosen grid: d_part holds `blocks` partials.
+cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
+                             const float *Q, int32_t n, int k, float b, int blocks,
+                             double *d_part, double *d_sum, cudaStream_t s);
 
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }

@@ -238,4 +238,12 @@ cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32
     return cudaGetLastError();
 }
 
+cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
+                             const float *Q, int32_t n, int k, float b, int blocks,
+                             double *d_part, double *d_sum, cudaStream_t s) {
+    rmse_kernel<<<blocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, P, (uint32_t)m, Q, (uint32_t)n, k, b, d_part);
+    sum_kernel<<<1, 32, 0, s>>>(d_part, blocks, d_sum);
+    return cudaGetLastError();
+}
+
 }  // namespace cumf

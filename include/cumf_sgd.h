@@ -252,6 +252,19 @@ int cumf_dev_rmse(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m
                   const float *d_Q, int32_t n, int k, float b, double *out_rmse,
                   void *stream);
 
+/* cumf_dev_rmse without any allocation.  No counterpart in the reference.  For callers that
+ * cannot allocate device memory when they evaluate (inside a fixed memory pool or arena,
+ * allocator hooks, out-of-memory handlers, code given only pre-sized buffers): the scratch
+ * is a fixed __device__ array inside the library (16385 doubles, held by every GPU that loads
+ * the library until exit), so nnz is limited to 134,217,728 ratings; larger calls return
+ * CUMF_ERR_ARG.  All calls share that array: calls whose kernels overlap on the GPU race and
+ * must be serialised by the caller.  The first call on each device (with that device
+ * current) looks up the array's address; make it before any stream capture.  Same inputs
+ * and output as cumf_dev_rmse. */
+int cumf_dev_rmse_noalloc(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m,
+                          const float *d_Q, int32_t n, int k, float b, double *out_rmse,
+                          void *stream);
+
 /* Device SM count and the default worker count (52 warps-worth of workers per SM,
  * README.md:61, scaled for the lane width in use). */
 int cumf_device_info(int gpu, int *sm_count, int *cc_major, int *cc_minor);
