@@ -45,8 +45,12 @@ cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int3
                               int *d_status, cudaStream_t stream, int *lanes_used);
 
 // ---- prep.cu ---------------------------------------------------------------------------
+// index_offset: element index of d[0] in the whole matrix (segments of modes B/C draw the
+// same values as the whole matrix would).
 cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,
-                                uint32_t tag, cudaStream_t s);
+                                uint32_t tag, cudaStream_t s, uint64_t index_offset = 0);
+// Seed of the sample stream of grid block g (block 0 keeps the run's seed).
+inline uint64_t block_seed(uint64_t seed, int g) { return seed + (uint64_t)g * 0x9E3779B97F4A7C15ull; }
 // Partial sums (sum r, sum r^2) per block into d_part[2*blocks]; returns blocks used.
 int stats_blocks(int64_t nnz);
 cudaError_t launch_rating_stats(const cumf_node *d_R, int64_t nnz, double *d_part,

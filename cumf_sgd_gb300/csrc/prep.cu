@@ -25,14 +25,14 @@ constexpr int kThreads = 256;
 constexpr int kReduceBlocks = 1024;  // fixed grid of the two-pass reductions
 
 template <int KIND>
-__global__ void init_kernel(void *out, uint64_t count, int k, uint64_t key) {
+__global__ void init_kernel(void *out, uint64_t count, int k, uint64_t key, uint64_t offset) {
     using S = Scalar<KIND>;
     typename S::T *o = reinterpret_cast<typename S::T *>(out);
     // (float)sqrt(1.0/k), the reference's scale (sgd.cu:519).
     const float scale = (float)sqrt(1.0 / (double)k);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        o[i] = S::from_float(__fmul_rn(init_uniform(key, i), scale));
+        o[i] = S::from_float(__fmul_rn(init_uniform(key, offset + i), scale));
     }
 }
 
@@ -177,15 +177,15 @@ int grid_for(uint64_t items, int per_thread = 1) {
 }  // namespace
 
 cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,
-                                uint32_t tag, cudaStream_t s) {
+                                uint32_t tag, cudaStream_t s, uint64_t index_offset) {
     const uint64_t count = (uint64_t)rows * (uint64_t)k;
     if (count == 0) return cudaSuccess;
     const uint64_t key = init_key(seed, tag);
     const int g = grid_for(count, 4);
     switch (store_of_precision(precision)) {
-        case kHalf: init_kernel<kHalf><<<g, kThreads, 0, s>>>(d, count, k, key); break;
-        case kBf16: init_kernel<kBf16><<<g, kThreads, 0, s>>>(d, count, k, key); break;
-        default: init_kernel<kFloat><<<g, kThreads, 0, s>>>(d, count, k, key); break;
+        case kHalf: init_kernel<kHalf><<<g, kThreads, 0, s>>>(d, count, k, key, index_offset); break;
+        case kBf16: init_kernel<kBf16><<<g, kThreads, 0, s>>>(d, count, k, key, index_offset); break;
+        default: init_kernel<kFloat><<<g, kThreads, 0, s>>>(d, count, k, key, index_offset); break;
     }
     return cudaGetLastError();
 }
