@@ -211,7 +211,7 @@ def main():
     train, test = synth.generate(spec, seed=rank, device="cuda")
     m, n, nnz = spec.m, spec.n, len(train)
     sm, _, _ = cm.device_info(local)
-    workers = args.workers or cm.default_workers(sm, K, args.precision, args.lanes)
+    workers = args.workers or cm.auto_workers(nnz, sm, K, args.precision, args.lanes)
     prec = args.precision
     eb = 4 if prec == "fp32" else 2
     dev = torch.device("cuda", local)

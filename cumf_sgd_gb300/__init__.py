@@ -51,6 +51,7 @@ class Parameter:
     verbose_epochs: bool = False
     prefetch: int = -1
     l2_hints: int = -1
+    ring: int = -1
 
     @property
     def ux(self) -> int:
@@ -65,7 +66,7 @@ class Parameter:
         _lib.check(_lib.load().cumf_default_params(C.byref(p)))
         for f in ("k", "num_workers", "u_grid", "v_grid", "x_grid", "y_grid", "num_iters", "gpu",
                   "lambda_p", "lambda_q", "lrate", "alpha", "beta", "seed", "lanes",
-                  "epochs_per_launch", "prefetch", "l2_hints"):
+                  "epochs_per_launch", "prefetch", "l2_hints", "ring"):
             setattr(p, f, getattr(self, f))
         p.precision = PRECISIONS[self.precision] if isinstance(self.precision, str) else int(self.precision)
         p.quiet = int(bool(self.quiet))
@@ -312,7 +313,13 @@ def device_info(gpu: int = 0):
 
 
 def default_workers(sm_count: int, k: int, precision: str = "fp16", lanes: int = 0) -> int:
+    """Resident workers (one wave) of the update kernel."""
     return int(_lib.load().cumf_default_workers(sm_count, k, PRECISIONS[precision], lanes))
+
+
+def auto_workers(nnz: int, sm_count: int, k: int, precision: str = "fp16", lanes: int = 0) -> int:
+    """Worker count the library picks for nnz ratings (three waves, >= 8 batches each)."""
+    return int(_lib.load().cumf_auto_workers(nnz, sm_count, k, PRECISIONS[precision], lanes))
 
 
 # ---- device-level entry points (integer device addresses, e.g. torch.Tensor.data_ptr()) ----
@@ -320,9 +327,9 @@ def default_workers(sm_count: int, k: int, precision: str = "fp16", lanes: int =
 def sgd_update(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, precision: str,
                num_workers: int, lanes: int, d_lr: int, first_epoch: int, n_epochs: int,
                lambda_p: float, lambda_q: float, seed: int, d_status: int = 0,
-               stream: int = 0, prefetch: int = -1, l2_hints: int = -1) -> None:
+               stream: int = 0, prefetch: int = -1, l2_hints: int = -1, ring: int = -1) -> None:
     """Batch-Hogwild epochs on caller-owned device buffers (sgd_kernel.cu:212-248)."""
-    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints)
+    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints, ring=ring)
     _lib.check(_lib.load().cumf_sgd_update_tuned(d_R, nnz, d_P, m, d_Q, n, k, PRECISIONS[precision],
                                                  num_workers, C.byref(t), d_lr, first_epoch, n_epochs,
                                                  lambda_p, lambda_q, seed, d_status or None,

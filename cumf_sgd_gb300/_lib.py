@@ -45,12 +45,12 @@ class Params(C.Structure):
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("lanes", C.c_int32),
                 ("quiet", C.c_int32), ("epochs_per_launch", C.c_int32),
                 ("verbose_epochs", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("reserved_", C.c_int32 * 3)]
+                ("ring", C.c_int32), ("reserved_", C.c_int32 * 2)]
 
 
 class Tuning(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("reserved_", C.c_int32 * 5)]
+                ("ring", C.c_int32), ("reserved_", C.c_int32 * 4)]
 
 
 class Model(C.Structure):
@@ -110,6 +110,7 @@ _SIGS = {
                                         C.POINTER(C.c_double), _VP]),
     "cumf_device_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cumf_default_workers": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "cumf_auto_workers": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int]),
     "cumf_random_map": (C.c_int, [C.c_uint32, C.c_int32, C.POINTER(C.c_int32)]),
     "cumf_grid_problem": (C.c_int, [C.POINTER(Node), C.c_int64, C.c_int32, C.c_int32, C.c_int, C.c_int,
                                     C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

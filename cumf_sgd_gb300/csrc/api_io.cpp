@@ -91,6 +91,7 @@ int cumf_default_params(cumf_params *p) {
     p->verbose_epochs = 0;
     p->prefetch = -1;
     p->l2_hints = -1;
+    p->ring = -1;
     return CUMF_OK;
 }
 

@@ -32,6 +32,7 @@ struct Tuning {
     int lanes = 0;      // 0 = default
     int prefetch = -1;  // -1 = default
     int hints = -1;     // -1 = default
+    int ring = -1;      // -1 = default, 0 = register prefetch kernel, 1 = shared-memory ring kernel
 };
 Tuning resolve_tuning(int k, int precision, Tuning t);
 int default_lanes(int k, int precision);

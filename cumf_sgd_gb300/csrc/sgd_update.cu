@@ -32,6 +32,7 @@ constexpr int kBlock = 256;   // threads per block
 constexpr int kMinBlocks = 4; // >= 1024 resident threads per SM (<= 64 registers)
 constexpr int kDefaultPrefetch = 2;
 constexpr int kDefaultHints = 1;
+constexpr int kDefaultRing = 0;
 constexpr int kBatch = 128;   // records per batch (update_vector_size, sgd_kernel.cu:198)
 // Records staged in shared memory at a time: 32, or 16 for narrow groups (keeps the
 // staging buffer of a 256-thread block under 27 KB).
@@ -262,15 +263,223 @@ sgd_hogwild_kernel(const UpdateArgs a) {
     if (bad && a.status != nullptr && lane == 0) atomicExch(a.status, (int)CUMF_ERR_RANGE);
 }
 
+
+// ---- deeper pipeline: rows staged asynchronously through a shared-memory ring ----------
+//
+// Same semantics as sgd_hogwild_kernel, with D records' rows in flight per worker instead
+// of one and no registers held for them: the rows of record x+D-1 are copied (cp.async,
+// 16 bytes per lane, L2 only) into ring slot (x+D-1) % D while record x is computed.  Each
+// lane only ever reads back its own slices, so the copy needs no cross-lane handoff.
+// In-order semantics per worker: a record whose row was written by one of the D-1 records
+// processed after its copy was issued takes the row from the previous record's registers
+// (distance 1) or re-reads it from global memory (distance 2..D-1).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int kRingDepth = 4;
+constexpr int kRingMinBlocks = 4;
+
+template <int K, int KIND, int G, int D>
+struct RingLayout {
+    static constexpr int SB = store_bytes(KIND);
+    static constexpr int ROW_WORDS = K * SB / 16;
+    static constexpr int GPB = kBlock / G;
+    static constexpr int kChunk = chunk_of(G);
+    static constexpr size_t rec_bytes = (size_t)GPB * 2 * 3 * (kChunk + 1) * 4;
+    static constexpr size_t rec_bytes_aligned = (rec_bytes + 15) / 16 * 16;
+    static constexpr size_t ring_bytes = (size_t)GPB * D * 2 * ROW_WORDS * 16;
+    static constexpr size_t smem = rec_bytes_aligned + ring_bytes;
+};
+
+template <int K, int KIND, int G, bool SR, int D>
+__global__ void __launch_bounds__(kBlock, kRingMinBlocks)
+sgd_ring_kernel(const UpdateArgs a) {
+    using C = Conv<KIND>;
+    using L = RingLayout<K, KIND, G, D>;
+    constexpr int ROW_WORDS = L::ROW_WORDS;
+    constexpr int NV = ROW_WORDS / G;
+    constexpr int GPB = L::GPB;
+    constexpr int kChunk = L::kChunk;
+    constexpr int CPB = kBatch / kChunk;
+    constexpr int WPL = kChunk * 3 / G;
+    static_assert(NV >= 1 && NV * G == ROW_WORDS, "lane split must cover the row");
+    static_assert(kChunk >= 2 * D - 1, "a staged chunk must land before its first use");
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typedef uint32_t RecBuf[2][3][kChunk + 1];
+    RecBuf *s_rec = reinterpret_cast<RecBuf *>(smem_raw);
+
+    const int lane = threadIdx.x % G;
+    const int gib = threadIdx.x / G;
+    const int worker = blockIdx.x * GPB + gib;
+    if (worker >= a.num_workers) return;
+    const unsigned gmask =
+        (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    uint4 *const ring = reinterpret_cast<uint4 *>(smem_raw + L::rec_bytes_aligned) +
+                        (size_t)gib * D * 2 * ROW_WORDS + lane * NV;
+
+    uint4 *const P = reinterpret_cast<uint4 *>(a.P) + lane * NV;
+    uint4 *const Q = reinterpret_cast<uint4 *>(a.Q) + lane * NV;
+    const uint32_t *const Rw = reinterpret_cast<const uint32_t *>(a.R);
+    const uint64_t nnz = a.nnz;
+    const float lp = a.lambda_p, lq = a.lambda_q;
+    const int chunks = a.batches * CPB;
+    const int total = chunks * kChunk;
+    const uint64_t pol_rec = l2_policy(a.hints != 0, false);
+    const uint64_t pol_row = l2_policy(a.hints != 0, true);
+    int bad = 0;
+
+    for (int ep = a.first_epoch; ep < a.first_epoch + a.n_epochs; ++ep) {
+        const float lr = __ldg(a.lr + ep);
+        const uint32_t round_key = (uint32_t)(splitmix64(a.seed ^ (kTagRound << 48)) + (uint64_t)ep);
+
+        auto fetch = [&](int t) {  // records of chunk t into buffer t & 1 (copies join the next group)
+            const uint64_t start = batch_start(a.seed, ep, worker, t / CPB, nnz);
+            uint64_t base = start + (uint64_t)((t % CPB) * kChunk);
+            while (base >= nnz) base -= nnz;
+#pragma unroll
+            for (int i = 0; i < WPL; ++i) {
+                const int word = lane + i * G;
+                uint64_t rec = base + (uint64_t)(word / 3);
+                while (rec >= nnz) rec -= nnz;
+                cp_async4(&s_rec[gib][t & 1][word % 3][word / 3], Rw + rec * 3 + (word % 3), pol_rec);
+            }
+        };
+        auto rec_field = [&](int x, int f) -> uint32_t { return s_rec[gib][(x / kChunk) & 1][f][x % kChunk]; };
+        auto issue = [&](int y) {  // rows of record y into slot y % D; always commits one group
+            if (y < total) {
+                const uint32_t uy = rec_field(y, 0), vy = rec_field(y, 1);
+                if ((uy < a.m) & (vy < a.n)) {
+                    uint4 *slot = ring + (size_t)(y % D) * 2 * ROW_WORDS;
+#pragma unroll
+                    for (int i = 0; i < NV; ++i) {
+                        cp_async16(slot + i, P + (uint64_t)uy * ROW_WORDS + i, pol_row);
+                        cp_async16(slot + ROW_WORDS + i, Q + (uint64_t)vy * ROW_WORDS + i, pol_row);
+                    }
+                }
+            }
+            cp_async_commit();
+        };
+
+        fetch(0);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncwarp(gmask);
+        if (chunks > 1) fetch(1);  // joins the first row group below
+#pragma unroll 1
+        for (int y = 0; y < D - 1; ++y) issue(y);
+
+        uint32_t pu[D - 1], pv[D - 1];
+#pragma unroll
+        for (int i = 0; i < D - 1; ++i) pu[i] = pv[i] = 0xffffffffu;
+        uint4 wp[NV], wq[NV];  // rows written by the previous record
+#pragma unroll
+        for (int i = 0; i < NV; ++i) wp[i] = wq[i] = make_uint4(0, 0, 0, 0);
+
+#pragma unroll 1
+        for (int x = 0; x < total; ++x) {
+            const int t = x / kChunk, j = x % kChunk;
+            if (j == 0 && t >= 1) {
+                __syncwarp(gmask);  // everyone is done with chunk t-1's buffer
+                if (t + 1 < chunks) fetch(t + 1);
+            }
+            if (j == kChunk - D + 1 && t + 1 < chunks) __syncwarp(gmask);  // chunk t+1 visible to all lanes
+            issue(x + D - 1);
+            cp_async_wait_group<D - 1>();  // this lane's slices of record x have landed
+
+            const uint32_t u = rec_field(x, 0), v = rec_field(x, 1);
+            const bool ok = (u < a.m) & (v < a.n);
+            if (ok) {
+                const float r = __uint_as_float(rec_field(x, 2));
+                const uint4 *slot = ring + (size_t)(x % D) * 2 * ROW_WORDS;
+                bool p_reload = false, q_reload = false;
+#pragma unroll
+                for (int i = 1; i < D - 1; ++i) {
+                    p_reload |= (u == pu[i]);
+                    q_reload |= (v == pv[i]);
+                }
+                uint4 fp[NV], fq[NV];
+#pragma unroll
+                for (int i = 0; i < NV; ++i) {
+                    fp[i] = (u == pu[0]) ? wp[i] : p_reload ? ld_row(P + (uint64_t)u * ROW_WORDS + i) : slot[i];
+                    fq[i] = (v == pv[0]) ? wq[i] : q_reload ? ld_row(Q + (uint64_t)v * ROW_WORDS + i) : slot[ROW_WORDS + i];
+                }
+                float s = 0.f;
+#pragma unroll
+                for (int i = 0; i < NV; ++i) {
+#pragma unroll
+                    for (int h = 0; h < C::kPairs; ++h) {
+                        const float2 pp = C::get(fp[i], h), qq = C::get(fq[i], h);
+                        s = __fmaf_rn(pp.x, qq.x, s);
+                        s = __fmaf_rn(pp.y, qq.y, s);
+                    }
+                }
+#pragma unroll
+                for (int o = G / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                const float err = r - s;
+                uint32_t key = 0;
+                if (SR) key = round_key ^ lowbias32((uint32_t)worker * (uint32_t)total + (uint32_t)x);
+#pragma unroll
+                for (int i = 0; i < NV; ++i) {
+                    const uint4 fpi = opaque(fp[i]), fqi = opaque(fq[i]);
+#pragma unroll
+                    for (int h = 0; h < C::kPairs; ++h) {
+                        const float2 pp = C::get(fpi, h), qq = C::get(fqi, h);
+                        const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
+                        const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
+                        const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
+                        const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
+                        if (SR) {
+                            const uint32_t pair = (uint32_t)(((lane * NV + i) * C::kPairs + h) * 2);
+                            C::put_sr(wp[i], h, px, py, lowbias32(key + pair));
+                            C::put_sr(wq[i], h, qx, qy, lowbias32(key + pair + 1u));
+                        } else {
+                            C::put(wp[i], h, px, py);
+                            C::put(wq[i], h, qx, qy);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < NV; ++i) {
+                    st_row_hint(P + (uint64_t)u * ROW_WORDS + i, wp[i], pol_row);
+                    st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
+                }
+            } else {
+                bad = 1;
+            }
+#pragma unroll
+            for (int i = D - 2; i >= 1; --i) {
+                pu[i] = pu[i - 1];
+                pv[i] = pv[i - 1];
+            }
+            pu[0] = ok ? u : 0xffffffffu;
+            pv[0] = ok ? v : 0xffffffffu;
+        }
+        cp_async_wait_all();
+        __syncwarp(gmask);
+    }
+    if (bad && a.status != nullptr && lane == 0) atomicExch(a.status, (int)CUMF_ERR_RANGE);
+}
+
 using KernelFn = void (*)(const UpdateArgs);
 
 struct KernelEntry {
     int k, kind, lanes;
     bool sr;
     KernelFn fn;
+    KernelFn ring;        // deeper-pipeline variant (nullptr where not built)
+    size_t ring_smem;     // its dynamic shared memory per block
 };
 
-#define CUMF_K(K, KIND, G, SR) {K, KIND, G, SR, &sgd_hogwild_kernel<K, KIND, G, SR>}
+#define CUMF_K(K, KIND, G, SR) {K, KIND, G, SR, &sgd_hogwild_kernel<K, KIND, G, SR>, \
+    &sgd_ring_kernel<K, KIND, G, SR, kRingDepth>, RingLayout<K, KIND, G, kRingDepth>::smem}
 #define CUMF_K_ALL_G(K, KIND, SR, G1, G2) CUMF_K(K, KIND, G1, SR), CUMF_K(K, KIND, G2, SR)
 
 // For each (k, storage) two lane widths: one 16-byte word per lane, or two.
@@ -329,13 +538,27 @@ bool lanes_supported(int k, int precision, int lanes) {
 
 int workers_per_block(int lanes) { return kBlock / lanes; }
 
+// The ring kernels need more than the default 48 KB of dynamic shared memory.
+cudaError_t prepare_ring(const KernelEntry *e) {
+    return cudaFuncSetAttribute(e->ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->ring_smem);
+}
+
+int resident_workers_of(const KernelEntry *e, bool ring, int sm_count) {
+    int blocks = 0;
+    if (ring) {
+        if (prepare_ring(e) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, e->ring, kBlock, e->ring_smem) != cudaSuccess)
+            return 0;
+    } else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, e->fn, kBlock, 0) != cudaSuccess) {
+        return 0;
+    }
+    return blocks * sm_count * (kBlock / e->lanes);
+}
+
 int resident_workers(int k, int precision, int lanes, int sm_count) {
     const KernelEntry *e = find_kernel(k, precision, lanes);
     if (!e) return 0;
-    int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, e->fn, kBlock, 0) != cudaSuccess)
-        return 0;
-    return blocks * sm_count * (kBlock / e->lanes);
+    return resident_workers_of(e, kDefaultRing != 0, sm_count);
 }
 
 Tuning resolve_tuning(int k, int precision, Tuning t) {
@@ -343,6 +566,7 @@ Tuning resolve_tuning(int k, int precision, Tuning t) {
     if (t.prefetch < 0) t.prefetch = kDefaultPrefetch;
     if (t.prefetch > 15) t.prefetch = 15;
     if (t.hints < 0) t.hints = kDefaultHints;
+    if (t.ring < 0) t.ring = kDefaultRing;
     return t;
 }
 
@@ -376,7 +600,13 @@ cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int3
     a.hints = t.hints;
     const int gpb = kBlock / e->lanes;
     const int blocks = (num_workers + gpb - 1) / gpb;
-    e->fn<<<blocks, kBlock, 0, stream>>>(a);
+    if (t.ring) {
+        cudaError_t ce = prepare_ring(e);
+        if (ce != cudaSuccess) return ce;
+        e->ring<<<blocks, kBlock, e->ring_smem, stream>>>(a);
+    } else {
+        e->fn<<<blocks, kBlock, 0, stream>>>(a);
+    }
     return cudaGetLastError();
 }
 

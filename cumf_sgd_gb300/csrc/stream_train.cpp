@@ -274,6 +274,7 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     tu.lanes = lanes;
     tu.prefetch = p.prefetch;
     tu.hints = p.l2_hints;
+    tu.ring = p.ring;
     int64_t step = 0;
     for (int it = 0; it < p.num_iters; ++it) {
         for (const Step &sp : sched[it]) {

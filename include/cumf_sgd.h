@@ -98,7 +98,8 @@ typedef struct cumf_params {
     int32_t verbose_epochs;    /* 1 = print one JSON line per epoch (needs a test set)  */
     int32_t prefetch;      /* L2 prefetch distance in records: -1 = tuned default, 0 = off */
     int32_t l2_hints;      /* L2 eviction hints: -1 = tuned default, 0 = off, 1 = on      */
-    int32_t reserved_[3];
+    int32_t ring;          /* update kernel pipeline (see cumf_tuning.ring)               */
+    int32_t reserved_[2];
 } cumf_params;
 
 /* Launch tuning of the update kernel (the knobs the autotuner searches). */
@@ -108,7 +109,10 @@ typedef struct cumf_tuning {
                               -1 = default, 0 = off, at most 15                          */
     int32_t l2_hints;      /* -1 = default, 0 = none, 1 = ratings evict_first and factor
                               rows evict_last                                            */
-    int32_t reserved_[5];
+    int32_t ring;          /* -1 = default, 0 = one record's rows in flight per worker (held
+                              in registers), 1 = four records' rows in flight, staged by
+                              cp.async in a shared-memory ring                            */
+    int32_t reserved_[4];
 } cumf_tuning;
 
 /* mf_model (singleGPU/sgd.h:110-138) as the model file holds it (main.cpp:247-266):
@@ -269,6 +273,9 @@ int cumf_dev_rmse_noalloc(const cumf_node *d_R, int64_t nnz, const float *d_P, i
  * README.md:61, scaled for the lane width in use). */
 int cumf_device_info(int gpu, int *sm_count, int *cc_major, int *cc_minor);
 int cumf_default_workers(int sm_count, int k, int precision, int lanes);
+/* Worker count for a problem of nnz ratings: three waves of resident workers (tail balance),
+ * at most nnz/1024 so every worker has at least eight 128-record batches per epoch. */
+int cumf_auto_workers(int64_t nnz, int sm_count, int k, int precision, int lanes);
 
 /* glibc-compatible id shuffle used for bit-exact layout parity: fills map[0..size) with
  * the permutation that srand(seed); random_shuffle(identity) produces
