@@ -170,6 +170,66 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision_suite(args):
+    """Precision sweep (BASELINE config 3): c3 planted matrix 1,000,990 x 624,961, 252.8M
+    train / 4.0M test ratings on 0..100, k=128, 20 epochs, for fp32 / fp16 / bf16 / bf16
+    with stochastic rounding / fp16 with stochastic rounding storage (fp32 arithmetic).
+    Full size: throughput and test RMSE per storage type.  Gap to the serial FP64 oracle:
+    on a 1% user subsample (users whose relabelled id is a multiple of 100), every GPU
+    variant and the FP64 oracle train the same sub-problem with the same worker count and
+    report test RMSE.  Prints one JSON line per measurement."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+    from oracle import oracle
+    build.build()
+    oracle.build_oracle()
+    spec = synth.C3 if args.scale >= 1.0 else synth.scaled(synth.C3, args.scale)
+    t0 = time.time()
+    train, test = synth.generate(spec, seed=0, device="cuda")
+    print(json.dumps({"suite": "precision", "event": "generated", "nnz": len(train), "secs": time.time() - t0}),
+          flush=True)
+    sm, _, _ = cm.device_info(0)
+    precs = ["fp32", "fp16", "bf16", "bf16sr", "fp16sr"]
+    epochs = args.e2e_epochs
+    if not args.no_e2e:
+        prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n, pinned=True)
+        tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+        for prec in precs:
+            W = cm.auto_workers(len(train), sm, K, prec)
+            par = cm.Parameter(k=K, num_workers=W, num_iters=epochs, alpha=0.08, beta=0.3, seed=1, gpu=0,
+                               precision=prec)
+            model, st = cm.sgd_train(prob, None, par, with_stats=True)
+            print(json.dumps({"suite": "precision", "config": "c3 full", "precision": prec, "workers": W,
+                              "epochs": epochs, "train_ms": st.train_ms,
+                              "updates_per_sec": len(train) * epochs / (st.train_ms * 1e-3),
+                              "test_rmse": cm.calc_rmse(tprob, model)}), flush=True)
+            del model
+        del prob
+    # 1% user subsample: compact user ids, keep item ids.
+    keep_tr = train["u"] % 100 == 0
+    keep_te = test["u"] % 100 == 0
+    sub_tr, sub_te = train[keep_tr].copy(), test[keep_te].copy()
+    sub_tr["u"] //= 100
+    sub_te["u"] //= 100
+    m_sub = (spec.m + 99) // 100
+    W = cm.auto_workers(len(sub_tr), sm, K, "fp16")
+    t0 = time.time()
+    P, Q, b = oracle.train_f64(sub_tr, m_sub, spec.n, k=K, num_workers=W, num_iters=epochs, alpha=0.08,
+                               beta=0.3, seed=1)
+    ref = oracle.calc_rmse_f64(sub_te, P, Q, b)
+    print(json.dumps({"suite": "precision", "config": "c3 1% users", "precision": "fp64 oracle (CPU, serial)",
+                      "nnz": len(sub_tr), "workers": W, "test_rmse": ref, "secs": time.time() - t0}), flush=True)
+    prob = cm.MFProblem.from_arrays(sub_tr["u"], sub_tr["v"], sub_tr["r"], m=m_sub, n=spec.n)
+    tprob = cm.MFProblem.from_arrays(sub_te["u"], sub_te["v"], sub_te["r"])
+    for prec in precs:
+        par = cm.Parameter(k=K, num_workers=W, num_iters=epochs, alpha=0.08, beta=0.3, seed=1, gpu=0,
+                           precision=prec)
+        r = cm.calc_rmse(tprob, cm.sgd_train(prob, None, par))
+        print(json.dumps({"suite": "precision", "config": "c3 1% users", "precision": prec, "workers": W,
+                          "test_rmse": r, "gap_to_fp64": r - ref}), flush=True)
+
+
 def _has_cuda():
     try:
         import torch
@@ -191,8 +251,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
-    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the c2 size (tests only)")
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
+    ap.add_argument("--suite", default="", choices=["", "precision"],
+                    help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
+    if args.suite == "precision":
+        run_precision_suite(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args)
         return

@@ -108,6 +108,8 @@ _SIGS = {
                                 C.POINTER(C.c_double), _VP]),
     "cumf_dev_rmse_noalloc": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, _VP, C.c_int32, C.c_int, C.c_float,
                                         C.POINTER(C.c_double), _VP]),
+    "cumf_tc_gemm": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, C.c_int, _VP,
+                               _VP, _VP]),
     "cumf_device_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cumf_default_workers": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "cumf_auto_workers": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int]),

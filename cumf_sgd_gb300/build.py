@@ -31,6 +31,7 @@ LIB_SOURCES = [
     "api_train.cpp",
     "stream_train.cpp",
     "noalloc.cu",
+    "tc_gemm.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp"}
 

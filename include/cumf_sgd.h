@@ -287,6 +287,16 @@ int cumf_random_map(uint32_t seed, int32_t size, int32_t *map);
 int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, int vy,
                       int64_t *grid_size, int64_t *u_seg, int64_t *v_seg);
 
+/* ---- warm-start MLP building blocks (no reference counterpart) -------------------- */
+/* BF16 tensor-core GEMM (tcgen05, fp32 accumulation in tensor memory):
+ *   out[M x N] = act(A[M x K] * B[N x K]^T + bias[N]),  A and B bf16 row-major,
+ * act 0 = identity, 1 = GELU (tanh form); out is bf16 (out_f32 = 0) or fp32 with row stride
+ * ldo; d_pre (may be NULL) receives the fp32 pre-activation.  K must be a multiple of 64;
+ * M and N are arbitrary.  d_status (may be NULL) receives CUMF_ERR_TIMEOUT if a bounded
+ * wait inside the kernel gives up. */
+int cumf_tc_gemm(const void *d_A, const void *d_B, int M, int N, int K, const float *d_bias, int act,
+                 void *d_out, int out_f32, int ldo, float *d_pre, int *d_status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -518,3 +518,65 @@ int or_train(or_train_args *a) {
     free(inv_p); free(inv_q);
     return 0;
 }
+
+/* ---- FP64 precision oracle ---------------------------------------------------------------- */
+
+void or_init_factors_f64(double *out, int64_t rows, int k, uint64_t seed, uint32_t tag) {
+    const uint64_t key = or_splitmix64(or_splitmix64(seed) + tag);
+    const double scale = sqrt(1.0 / (double)k);
+    const int64_t count = rows * (int64_t)k;
+    for (int64_t i = 0; i < count; i++) out[i] = (double)init_uniform(key, (uint64_t)i) * scale;
+}
+
+static void run_batch_f64(or_sgd64_args *a, int ep, int w, int64_t b, double lr) {
+    const uint64_t start = or_batch_start(a->seed, (uint32_t)ep, (uint32_t)w, (uint32_t)b, (uint64_t)a->nnz);
+    const int k = a->k;
+    for (int i = 0; i < 128; i++) {
+        const or_node x = a->R[(start + (uint64_t)i) % (uint64_t)a->nnz];
+        if ((uint32_t)x.u >= (uint32_t)a->m || (uint32_t)x.v >= (uint32_t)a->n) continue;
+        double *p = a->P + (int64_t)x.u * k, *q = a->Q + (int64_t)x.v * k;
+        double dot = 0;
+        for (int d = 0; d < k; d++) dot += p[d] * q[d];
+        const double err = (double)x.r * a->rscale - dot;
+        for (int d = 0; d < k; d++) {
+            const double pp = p[d], qq = q[d];
+            p[d] = pp + lr * (err * qq - a->lambda_p * pp);
+            q[d] = qq + lr * (err * pp - a->lambda_q * qq);
+        }
+    }
+}
+
+void or_sgd_epochs_f64(or_sgd64_args *a) {
+    if (a->nnz <= 0 || a->num_workers <= 0) return;
+    const int64_t per = (int64_t)a->num_workers * 128;
+    const int64_t batches = (a->nnz + per - 1) / per;
+    for (int ep = a->first_epoch; ep < a->first_epoch + a->n_epochs; ep++) {
+        const double lr = a->lr[ep];
+        if (a->order == OR_ORDER_WORKER_MAJOR) {
+            for (int w = 0; w < a->num_workers; w++)
+                for (int64_t b = 0; b < batches; b++) run_batch_f64(a, ep, w, b, lr);
+        } else {
+            for (int64_t b = 0; b < batches; b++)
+                for (int w = 0; w < a->num_workers; w++) run_batch_f64(a, ep, w, b, lr);
+        }
+    }
+}
+
+double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t m, const double *Q,
+                        int32_t n, int k, double b) {
+    if (nnz == 0) return 0;
+    double loss = 0;
+    for (int64_t i = 0; i < nnz; i++) {
+        const int32_t u = R[i].u, v = R[i].v;
+        double z = b;
+        if (u >= 0 && u < m && v >= 0 && v < n) {
+            const double *p = P + (int64_t)u * k, *q = Q + (int64_t)v * k;
+            z = 0;
+            for (int d = 0; d < k; d++) z += p[d] * q[d];
+            if (isnan(z)) z = b;
+        }
+        const double e = (double)R[i].r - z;
+        loss += e * e;
+    }
+    return sqrt(loss / (double)nnz);
+}

@@ -123,6 +123,31 @@ typedef struct or_train_args {
 } or_train_args;
 int or_train(or_train_args *a);
 
+/* Serial FP64 SGD (the precision oracle): the same batch schedule as or_sgd_epochs, double
+ * factors and arithmetic, no storage rounding. */
+typedef struct or_sgd64_args {
+    const or_node *R;
+    int64_t nnz;
+    double *P;
+    int32_t m;
+    double *Q;
+    int32_t n;
+    int k;
+    int num_workers;
+    int order;
+    const double *lr;
+    int first_epoch, n_epochs;
+    double lambda_p, lambda_q;
+    double rscale;       /* ratings are used as r * rscale (in double) */
+    uint64_t seed;
+} or_sgd64_args;
+void or_sgd_epochs_f64(or_sgd64_args *a);
+/* FP64 factor init: U(0,1] * sqrt(1/k) in double with the same uniforms as or_init_factors. */
+void or_init_factors_f64(double *out, int64_t rows, int k, uint64_t seed, uint32_t tag);
+/* RMSE of an FP64 model (double dot and error). */
+double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t m, const double *Q,
+                        int32_t n, int k, double b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,6 +75,14 @@ class _TrainArgs(C.Structure):
                 ("std_dev", C.c_float)]
 
 
+class _Sgd64Args(C.Structure):
+    _fields_ = [("R", C.c_void_p), ("nnz", C.c_int64), ("P", C.c_void_p), ("m", C.c_int32),
+                ("Q", C.c_void_p), ("n", C.c_int32), ("k", C.c_int), ("num_workers", C.c_int),
+                ("order", C.c_int), ("lr", C.c_void_p), ("first_epoch", C.c_int), ("n_epochs", C.c_int),
+                ("lambda_p", C.c_double), ("lambda_q", C.c_double), ("rscale", C.c_double),
+                ("seed", C.c_uint64)]
+
+
 _lib = None
 
 
@@ -107,6 +115,11 @@ def lib() -> C.CDLL:
         _lib.or_train.argtypes = [C.POINTER(_TrainArgs)]
         _lib.or_shuffle_model.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int]
         _lib.or_scale_model.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_float]
+        _lib.or_sgd_epochs_f64.argtypes = [C.POINTER(_Sgd64Args)]
+        _lib.or_init_factors_f64.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_uint32]
+        _lib.or_calc_rmse_f64.restype = C.c_double
+        _lib.or_calc_rmse_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                          C.c_int, C.c_double]
         _lib.or_hogwild_threads.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
                                             C.c_int32, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
                                             C.c_float, C.c_float, C.c_uint64, C.c_int]
@@ -254,3 +267,34 @@ def ref_rmse(test_path: str, model_path: str) -> float:
         if line.startswith("RMSE_FULL"):
             return float(line.split()[1])
     raise RuntimeError("ref_rmse printed no RMSE")
+
+
+def train_f64(records: np.ndarray, m: int, n: int, k: int = 128, num_workers: int = 1, num_iters: int = 20,
+              lambda_p: float = 0.05, lambda_q: float = 0.05, alpha: float = 0.08, beta: float = 0.3,
+              lrate: float = 0.0, seed: int = 0, order: int = OR_ORDER_ROUND_ROBIN):
+    """Serial FP64 sgd_train (mode A): the same statistics, id maps, sample schedule and
+    learning-rate table as the GPU path, everything else in double.  Returns (P, Q, b) with
+    float64 factors (unscaled, un-permuted)."""
+    rec = np.ascontiguousarray(records).copy()
+    ave, std = collect_data(rec)
+    scale = max(1e-4, float(np.float32(std)))
+    pm, qm = gen_random_map(seed, m), gen_random_map(seed, n)
+    rec["u"], rec["v"] = pm[rec["u"]], qm[rec["v"]]
+    P = np.zeros((m, k), dtype=np.float64)
+    Q = np.zeros((n, k), dtype=np.float64)
+    lib().or_init_factors_f64(_ptr(P), m, k, seed, 1)
+    lib().or_init_factors_f64(_ptr(Q), n, k, seed, 2)
+    lr = np.array([alpha / (1 + beta * i ** 1.5) + lrate for i in range(num_iters + 4)], dtype=np.float64)
+    a = _Sgd64Args(R=_ptr(rec), nnz=len(rec), P=_ptr(P), m=m, Q=_ptr(Q), n=n, k=k, num_workers=num_workers,
+                   order=order, lr=_ptr(lr), first_epoch=0, n_epochs=num_iters, lambda_p=lambda_p / scale,
+                   lambda_q=lambda_q / scale, rscale=1.0 / scale, seed=seed)
+    lib().or_sgd_epochs_f64(C.byref(a))
+    f = np.sqrt(scale)
+    return P[pm] * f, Q[qm] * f, float(ave) / float(std)
+
+
+def calc_rmse_f64(records: np.ndarray, P: np.ndarray, Q: np.ndarray, b: float) -> float:
+    rec = np.ascontiguousarray(records)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    return lib().or_calc_rmse_f64(_ptr(rec), len(rec), _ptr(P), P.shape[0], _ptr(Q), Q.shape[0], P.shape[1], b)
