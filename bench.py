@@ -230,6 +230,140 @@ def run_precision_suite(args):
                           "test_rmse": r, "gap_to_fp64": r - ref}), flush=True)
 
 
+def run_warmstart_suite(args):
+    """Learned warm start (BASELINE config 5, and the c2-shape headline with --scale-c2).
+
+    Scenario: a deployed model exists for a base matrix; 50,000 new users arrive with ratings
+    amounting to 5% of the base train count (one planted model for all users, seeded).
+      1. MLP training data: 8 plain-SGD solves (fp16, 20 epochs) of c1-shaped planted
+         matrices with different seeds; per user, features from (ratings, solved Q), target
+         the solved P row.  The MLP trains on the tensor cores (cumf_mlp_train).
+      2. Base model: plain fp16 SGD on the base matrix (not timed: it is the deployed model).
+      3. Target: the serial FP64 oracle trained from scratch on the grown matrix for 20
+         epochs; target = its test RMSE + 0.002.
+      4. Cold start: plain fp16 SGD from random init on the grown matrix.
+         Warm start: base P for old users, MLP(features) for new users, base Q; bf16 with
+         stochastic rounding; time includes feature extraction and MLP inference.
+         Ablation: the same warm start with random new-user rows (no MLP).
+    Time-to-target = cumulative CUDA-event training time up to the first epoch whose test
+    RMSE <= target (evaluation excluded), plus the warm start's own preparation time."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+    from oracle import oracle
+    build.build()
+    oracle.build_oracle()
+    dev = torch.device("cuda", 0)
+    sm, _, _ = cm.device_info(0)
+    big = args.scale >= 2.0
+    base_spec = synth.C2 if big else synth.C1
+    new_users = 50_000
+    epochs = args.e2e_epochs
+    out = lambda d: print(json.dumps({"suite": "warmstart", "shape": "c2" if big else "c1", **d}), flush=True)
+
+    def solve(tr, m, n, seed, precision="fp16", iters=20, init=None, te=None, alpha=0.08):
+        prob = cm.MFProblem.from_arrays(tr["u"], tr["v"], tr["r"], m=m, n=n)
+        tprob = cm.MFProblem.from_arrays(te["u"], te["v"], te["r"]) if te is not None else None
+        W = cm.auto_workers(len(tr), sm, K, precision)
+        par = cm.Parameter(k=K, num_workers=W, num_iters=iters, alpha=alpha, beta=0.3, seed=seed, gpu=0,
+                           precision=precision)
+        return cm.sgd_train_ex(prob, tprob, par, init)
+
+    def features(tr, m, n, Q):
+        dR = torch.from_numpy(tr.view(np.uint8).copy()).to(dev)
+        dQ = torch.from_numpy(np.ascontiguousarray(Q)).to(dev)
+        dX = torch.empty(m, K + 3, device=dev)
+        cm.user_features(dR.data_ptr(), len(tr), dQ.data_ptr(), n, K, m, dX.data_ptr())
+        return dX
+
+    # 1. MLP training data from 8 solves of the same family
+    t0 = time.time()
+    Xs, Ts = [], []
+    for s in range(8):
+        tr, _ = synth.generate(base_spec, seed=10 + s, device="cuda")
+        model, _, _, _ = solve(tr, base_spec.m, base_spec.n, seed=10 + s)
+        X = features(tr, base_spec.m, base_spec.n, model.Q)
+        deg = np.bincount(tr["u"], minlength=base_spec.m)
+        keep = torch.from_numpy(np.nonzero(deg > 0)[0]).to(dev)
+        Xs.append(X[keep])
+        Ts.append(torch.from_numpy(np.ascontiguousarray(model.P)).to(dev)[keep])
+    X = torch.cat(Xs).contiguous()
+    T = torch.cat(Ts).contiguous()
+    mlp = cm.MLP(K + 3, 512, K, seed=7)
+    loss0 = mlp.loss_grad(X.data_ptr(), T.data_ptr(), len(X))
+    torch.cuda.synchronize()
+    t1 = time.time()
+    loss = mlp.train(X.data_ptr(), T.data_ptr(), len(X), epochs=args.mlp_epochs, batch=4096 if big else 1024,
+                     lr=1e-3, seed=3)
+    torch.cuda.synchronize()
+    out({"event": "mlp_trained", "rows": len(X), "loss_before": loss0, "loss_after": loss,
+         "train_s": time.time() - t1, "data_s": t1 - t0})
+
+    # 2. base + growth from one planted model
+    b_tr, b_te, n_tr, n_te = synth.generate_growth(base_spec, new_users, 0.05, seed=100, device="cuda")
+    m_all, n = base_spec.m + new_users, base_spec.n
+    base_model, _, _, _ = solve(b_tr, base_spec.m, n, seed=1)
+    g_tr = np.concatenate([b_tr, n_tr])
+    g_te = np.concatenate([b_te, n_te])
+    out({"event": "data", "base_train": len(b_tr), "new_train": len(n_tr), "test": len(g_te),
+         "new_test": len(n_te), "users": m_all, "items": n})
+
+    # 3. FP64 oracle target (c1 shape; at c2 shape the target is cold fp16's 20-epoch RMSE)
+    if not big:
+        t0 = time.time()
+        W = cm.auto_workers(len(g_tr), sm, K, "fp16")
+        P64, Q64, b64 = oracle.train_f64(g_tr, m_all, n, k=K, num_workers=W, num_iters=20, seed=5)
+        oracle_rmse = oracle.calc_rmse_f64(g_te, P64, Q64, b64)
+        target = oracle_rmse + 0.002
+        out({"event": "oracle", "fp64_test_rmse": oracle_rmse, "target": target, "secs": time.time() - t0})
+
+    def time_to_target(rm, ms, target):
+        for e in range(len(rm)):
+            if rm[e] <= target:
+                return float(ms[e]), e + 1
+        return None, None
+
+    # 4. cold start
+    _, cst, crm, cms = solve(g_tr, m_all, n, seed=5, precision="fp16", iters=epochs, te=g_te)
+    if big:
+        target = float(crm[-1]) + 0.002
+        out({"event": "target", "definition": "cold fp16 RMSE after %d epochs + 0.002" % epochs, "target": target})
+    cold_ms, cold_ep = time_to_target(crm, cms, target)
+    out({"arm": "cold fp16", "epoch_rmse": [round(x, 5) for x in crm], "epoch_ms": [round(x, 3) for x in cms],
+         "time_to_target_ms": cold_ms, "epochs_to_target": cold_ep})
+
+    # warm start: features + MLP inference for every user (timed), base rows for old users
+    def warm(use_mlp):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        P0 = np.zeros((m_all, K), dtype=np.float32)
+        P0[: base_spec.m] = base_model.P
+        if use_mlp:
+            Xg = features(g_tr, m_all, n, base_model.Q)
+            Y = torch.empty(m_all, K, device=dev)
+            mlp.forward(Xg.data_ptr(), m_all, Y.data_ptr())
+            P0[base_spec.m:] = Y[base_spec.m:].cpu().numpy()
+        else:
+            P0[base_spec.m:] = oracle.init_factors(new_users, K, "fp32", 9, 1)
+        init = cm.MFModel.from_arrays(P0, base_model.Q, base_model.b)
+        prep_ms = (time.perf_counter() - t0) * 1e3
+        _, wst, wrm, wms = solve(g_tr, m_all, n, seed=5, precision="bf16sr", iters=epochs, init=init, te=g_te,
+                                 alpha=args.warm_alpha)
+        new_prob = cm.MFProblem.from_arrays(n_te["u"], n_te["v"], n_te["r"])
+        init_rmse_new = cm.calc_rmse(new_prob, init)
+        return prep_ms, wrm, wms, init_rmse_new
+
+    for use_mlp in (True, False):
+        prep_ms, wrm, wms, init_new = warm(use_mlp)
+        w_ms, w_ep = time_to_target(wrm, wms, target)
+        total = None if w_ms is None else w_ms + prep_ms
+        out({"arm": "warm bf16sr" + ("" if use_mlp else " (no MLP: random new users)"),
+             "prep_ms": prep_ms, "new_user_test_rmse_at_init": init_new,
+             "epoch_rmse": [round(x, 5) for x in wrm], "epoch_ms": [round(x, 3) for x in wms],
+             "time_to_target_ms": total, "epochs_to_target": w_ep,
+             "speedup_vs_cold": (cold_ms / total) if (cold_ms and total) else None})
+
+
 def _has_cuda():
     try:
         import torch
@@ -252,11 +386,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
-    ap.add_argument("--suite", default="", choices=["", "precision"],
+    ap.add_argument("--mlp-epochs", type=int, default=30)
+    ap.add_argument("--warm-alpha", type=float, default=0.02, help="initial learning rate of warm refinement")
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
     if args.suite == "precision":
         run_precision_suite(args)
+        return
+    if args.suite == "warmstart":
+        run_warmstart_suite(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

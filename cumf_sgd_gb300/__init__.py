@@ -368,3 +368,73 @@ def dev_rmse(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, b: 
     _lib.check(_lib.load().cumf_dev_rmse(d_R, nnz, d_P, m, d_Q, n, k, b, C.byref(out),
                                          stream or None))
     return out.value
+
+
+# ---- learned warm start -----------------------------------------------------------------
+
+class MLP:
+    """The warm-start encoder: d_in -> hidden -> hidden -> d_out (GELU), bf16 on the tensor
+    cores with fp32 master weights (cumf_mlp_* in the C ABI).  Device arrays are passed as
+    integer addresses (e.g. torch.Tensor.data_ptr())."""
+
+    def __init__(self, d_in: int, hidden: int = 512, d_out: int = 128, seed: int = 0):
+        h = C.c_void_p()
+        _lib.check(_lib.load().cumf_mlp_create(d_in, hidden, d_out, seed, C.byref(h)))
+        self._h = h
+        self.d_in, self.hidden, self.d_out = d_in, hidden, d_out
+
+    def param_count(self) -> int:
+        return int(_lib.load().cumf_mlp_param_count(self._h))
+
+    def get(self, which: int = 0) -> np.ndarray:
+        out = np.zeros(self.param_count(), dtype=np.float32)
+        _lib.check(_lib.load().cumf_mlp_get_params(self._h, out.ctypes.data, len(out), which))
+        return out
+
+    def set(self, params: np.ndarray) -> None:
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        _lib.check(_lib.load().cumf_mlp_set_params(self._h, params.ctypes.data, len(params)))
+
+    def forward(self, d_X: int, rows: int, d_Y: int, stream: int = 0) -> None:
+        _lib.check(_lib.load().cumf_mlp_forward(self._h, d_X, rows, d_Y, stream or None))
+
+    def loss_grad(self, d_X: int, d_T: int, rows: int, stream: int = 0) -> float:
+        loss = C.c_double()
+        _lib.check(_lib.load().cumf_mlp_loss_grad(self._h, d_X, d_T, rows, C.byref(loss), stream or None))
+        return loss.value
+
+    def train(self, d_X: int, d_T: int, rows: int, epochs: int, batch: int = 1024, lr: float = 1e-3,
+              seed: int = 0, stream: int = 0) -> float:
+        loss = C.c_double()
+        _lib.check(_lib.load().cumf_mlp_train(self._h, d_X, d_T, rows, epochs, batch, lr, seed, C.byref(loss),
+                                              stream or None))
+        return loss.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().cumf_mlp_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def user_features(d_R: int, nnz: int, d_Q: int, n: int, k: int, m: int, d_X: int, stream: int = 0) -> None:
+    """Warm-start features of m users (m x (k+3), fp32) from device ratings and fp32 Q."""
+    _lib.check(_lib.load().cumf_user_features(d_R, nnz, d_Q, n, k, m, d_X, stream or None))
+
+
+def sgd_train_ex(tr: MFProblem, te: Optional[MFProblem], param: Parameter, init: Optional[MFModel] = None):
+    """sgd_train with optional starting factors and per-epoch test RMSE; returns
+    (model, stats, epoch_rmse, epoch_cumulative_train_ms)."""
+    out = _lib.Model()
+    st = _lib.TrainStats()
+    p = param.to_c()
+    rm = np.full(max(1, param.num_iters), np.nan)
+    ms = np.full(max(1, param.num_iters), np.nan)
+    rc = _lib.load().cumf_train_ex(C.byref(tr._c), C.byref(te._c) if te is not None else None, C.byref(p),
+                                   C.byref(init._c) if init is not None else None, C.byref(out), C.byref(st),
+                                   rm.ctypes.data, ms.ctypes.data)
+    _lib.check(rc)
+    stats = TrainStats(**{f: getattr(st, f) for f, _ in _lib.TrainStats._fields_ if f != "reserved_"})
+    return MFModel(out), stats, rm[:param.num_iters], ms[:param.num_iters]

@@ -110,6 +110,18 @@ _SIGS = {
                                         C.POINTER(C.c_double), _VP]),
     "cumf_tc_gemm": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, C.c_int, _VP,
                                _VP, _VP]),
+    "cumf_user_features": (C.c_int, [_VP, C.c_int64, _VP, C.c_int32, C.c_int, C.c_int32, _VP, _VP]),
+    "cumf_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "cumf_mlp_destroy": (C.c_int, [_VP]),
+    "cumf_mlp_param_count": (C.c_int64, [_VP]),
+    "cumf_mlp_get_params": (C.c_int, [_VP, _VP, C.c_int64, C.c_int]),
+    "cumf_mlp_set_params": (C.c_int, [_VP, _VP, C.c_int64]),
+    "cumf_mlp_forward": (C.c_int, [_VP, _VP, C.c_int64, _VP, _VP]),
+    "cumf_mlp_loss_grad": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.POINTER(C.c_double), _VP]),
+    "cumf_mlp_train": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64,
+                                 C.POINTER(C.c_double), _VP]),
+    "cumf_train_ex": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Model),
+                                C.POINTER(Model), C.POINTER(TrainStats), _VP, _VP]),
     "cumf_device_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cumf_default_workers": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "cumf_auto_workers": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int]),

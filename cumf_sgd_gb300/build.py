@@ -32,6 +32,7 @@ LIB_SOURCES = [
     "stream_train.cpp",
     "noalloc.cu",
     "tc_gemm.cu",
+    "mlp.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp"}
 

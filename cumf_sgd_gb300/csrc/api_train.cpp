@@ -80,7 +80,8 @@ struct EpochEval {
 };
 
 int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_params &p,
-                 int workers, int lanes, cumf_model *out, cumf_train_stats *st) {
+                 int workers, int lanes, cumf_model *out, cumf_train_stats *st,
+                 const cumf_model *init = nullptr, double *epoch_rmse = nullptr, double *epoch_ms = nullptr) {
     const double t0 = now_ms();
     const int64_t nnz = tr->nnz;
     const int32_t m = tr->m, n = tr->n;
@@ -124,6 +125,21 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(d_Q.alloc((size_t)n * k * eb));
     CUMF_CUDA(launch_init_factors(d_P.p, m, k, p.precision, p.seed, 1, s));
     CUMF_CUDA(launch_init_factors(d_Q.p, n, k, p.precision, p.seed, 2, s));
+    if (init) {  // starting factors for the first init->m users and init->n items
+        const float f0 = (float)sqrt(pr.scale);
+        const int64_t mi = std::min<int64_t>(init->m, m), ni = std::min<int64_t>(init->n, n);
+        DevBuf tmp;
+        CUMF_CUDA(tmp.alloc((size_t)std::max(mi, ni) * k * sizeof(float)));
+        if (mi > 0) {
+            CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->P, (size_t)mi * k * sizeof(float), cudaMemcpyHostToDevice, s));
+            CUMF_CUDA(launch_import(tmp.as<float>(), d_pmap.as<int32_t>(), mi, k, f0, d_P.p, p.precision, s));
+        }
+        if (ni > 0) {
+            CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->Q, (size_t)ni * k * sizeof(float), cudaMemcpyHostToDevice, s));
+            CUMF_CUDA(launch_import(tmp.as<float>(), d_qmap.as<int32_t>(), ni, k, f0, d_Q.p, p.precision, s));
+        }
+        CUMF_CUDA(cudaStreamSynchronize(s));
+    }
 
     std::vector<float> lr(std::max(1, p.num_iters + 4));
     cumf_lr_schedule(p.alpha, p.beta, p.lrate, (int)lr.size(), lr.data());
@@ -133,7 +149,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     const float factor = (float)sqrt(pr.scale);  // scale_model (sgd.cu:598)
     const float b = pr.ave / pr.std_dev;           // model->b (sgd.cu:679)
     EpochEval ev;
-    const bool per_epoch = p.verbose_epochs && va && va->nnz > 0;
+    const bool per_epoch = (p.verbose_epochs || epoch_rmse || epoch_ms) && va && va->nnz > 0;
     if (per_epoch) {
         if (int rc = ev.init(va, m, n, k, s)) return rc;
     }
@@ -175,9 +191,13 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
             double rmse = 0;
             if (int rc = ev.eval(d_P.p, d_Q.p, p.precision, d_pmap.as<int32_t>(), d_qmap.as<int32_t>(), factor, b, s, &rmse))
                 return rc;
-            printf("{\"epoch\": %d, \"train_ms\": %.3f, \"elapsed_ms\": %.3f, \"test_rmse\": %.6f}\n", ep + cnt, ms,
-                   train_ms, rmse);
-            fflush(stdout);
+            if (epoch_rmse) epoch_rmse[ep] = rmse;
+            if (epoch_ms) epoch_ms[ep] = train_ms;
+            if (p.verbose_epochs) {
+                printf("{\"epoch\": %d, \"train_ms\": %.3f, \"elapsed_ms\": %.3f, \"test_rmse\": %.6f}\n", ep + cnt,
+                       ms, train_ms, rmse);
+                fflush(stdout);
+            }
         }
     }
     int status = 0;
@@ -285,6 +305,27 @@ int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params
     }
     if (p.ux * p.vy == 1) return train_mode_a(tr, va, p, workers, lanes, out, stats);
     return stream_train(tr, p, workers, lanes, out, stats);
+}
+
+int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_params *params,
+                  const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
+                  double *epoch_ms) {
+    if (!tr || !out) return fail(CUMF_ERR_ARG, "train_ex: problem and model must not be NULL");
+    if (tr->nnz < 0 || (tr->nnz > 0 && !tr->R) || tr->m < 1 || tr->n < 1)
+        return fail(CUMF_ERR_ARG, "train_ex: malformed problem");
+    memset(out, 0, sizeof(*out));
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (int rc = check_params(params)) return rc;
+    cumf_params p = *params;
+    if (p.u_grid * p.v_grid != 1) return fail(CUMF_ERR_ARG, "train_ex: only u = v = 1 (the whole problem in HBM)");
+    p.x_grid = p.y_grid = 1;
+    p.ux = p.vy = 1;
+    if (init && (init->k != p.k || (init->m > 0 && !init->P) || (init->n > 0 && !init->Q)))
+        return fail(CUMF_ERR_ARG, "train_ex: init model does not match k");
+    if (int rc = select_device(p.gpu)) return rc;
+    const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    if (!p.quiet) print_args(p);
+    return train_mode_a(tr, te, p, p.num_workers, lanes, out, stats, init, epoch_rmse, epoch_ms);
 }
 
 int cumf_rmse(const cumf_problem *te, const cumf_model *model, double *out) {

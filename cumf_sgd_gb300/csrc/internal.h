@@ -61,6 +61,9 @@ cudaError_t launch_shuffle_scale(const cumf_node *in, cumf_node *out, int64_t nn
                                  int32_t n, float scale, int *d_status, cudaStream_t s);
 cudaError_t launch_export(const void *in, int precision, const int32_t *map, int64_t rows,
                           int k, float factor, float *out, cudaStream_t s);
+// dst[map[o]] = storage(src[o] / factor): starting factors in storage layout.
+cudaError_t launch_import(const float *src, const int32_t *map, int64_t rows, int k, float factor, void *dst,
+                          int precision, cudaStream_t s);
 int rmse_blocks(int64_t nnz);
 cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
                         const float *Q, int32_t n, int k, float b, double *d_part,

@@ -112,6 +112,20 @@ __global__ void export_kernel(const void *in, const int32_t *map, uint64_t rows,
     }
 }
 
+// dst[map[o]] = storage(src[o] / factor) for o < rows: the inverse of the export.
+template <int KIND>
+__global__ void import_kernel(const float *src, const int32_t *map, uint64_t rows, int k, float factor, void *dst) {
+    using S = Scalar<KIND>;
+    typename S::T *d = reinterpret_cast<typename S::T *>(dst);
+    const uint64_t count = rows * (uint64_t)k;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t o = i / (uint64_t)k, j = i - o * (uint64_t)k;
+        const uint64_t drow = map ? (uint64_t)(uint32_t)map[o] : o;
+        d[drow * (uint64_t)k + j] = S::from_float(__fdiv_rn(src[i], factor));
+    }
+}
+
 // Eight lanes per rating; float dot in fp32, squared error rounded to fp32 and summed in
 // fp64 as calc_rmse does (`mf_float e = r - z; loss += e*e;`, mf.cpp:3831-3834).
 constexpr int kRmseLanes = 8;
@@ -235,6 +249,19 @@ cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32
     rmse_kernel<<<kReduceBlocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, P, (uint32_t)m, Q,
                                                    (uint32_t)n, k, b, d_part);
     sum_kernel<<<1, 32, 0, s>>>(d_part, kReduceBlocks, d_sum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_import(const float *src, const int32_t *map, int64_t rows, int k, float factor, void *dst,
+                          int precision, cudaStream_t s) {
+    const uint64_t count = (uint64_t)rows * (uint64_t)k;
+    if (count == 0) return cudaSuccess;
+    const int g = grid_for(count, 4);
+    switch (store_of_precision(precision)) {
+        case kHalf: import_kernel<kHalf><<<g, kThreads, 0, s>>>(src, map, rows, k, factor, dst); break;
+        case kBf16: import_kernel<kBf16><<<g, kThreads, 0, s>>>(src, map, rows, k, factor, dst); break;
+        default: import_kernel<kFloat><<<g, kThreads, 0, s>>>(src, map, rows, k, factor, dst); break;
+    }
     return cudaGetLastError();
 }
 

@@ -140,3 +140,46 @@ def generate(spec: PlantedSpec, seed: int = 0, device: Optional[str] = None,
 
 def generate_c1(seed: int = 0, device: Optional[str] = None):
     return generate(C1, seed, device)
+
+
+def generate_growth(spec: PlantedSpec, new_users: int, new_frac: float, seed: int = 0,
+                    device: Optional[str] = None, test_frac: float = 0.1, chunk: int = 1 << 24):
+    """A base matrix plus growth from one planted model: users [0, spec.m) are the base users
+    (Zipf, as `generate`), users [spec.m, spec.m + new_users) are new users drawn uniformly,
+    whose ratings add `new_frac` of the base train count.  Returns
+    (base_train, base_test, new_train, new_test); tests hold `test_frac` of each part."""
+    device = torch.device(device or ("cuda" if torch.cuda.is_available() else "cpu"))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    m_all = spec.m + new_users
+    total = spec.nnz_train + spec.nnz_test
+    us = spec.user_s if spec.user_s >= 0 else fit_zipf_exponent(spec.m, total, spec.top_user)
+    its = spec.item_s if spec.item_s >= 0 else fit_zipf_exponent(spec.n, total, spec.top_item)
+    ucdf, urel = _zipf_sampler(spec.m, us, gen, device)
+    icdf, irel = _zipf_sampler(spec.n, its, gen, device)
+    sd = math.sqrt(spec.factor_var)
+    P = torch.randn(m_all, spec.rank, generator=gen, device=device) * sd
+    Q = torch.randn(spec.n, spec.rank, generator=gen, device=device) * sd
+
+    def block(count: int, new: bool) -> np.ndarray:
+        out = np.empty(count, dtype=NODE_DTYPE)
+        for a in range(0, count, chunk):
+            b = min(count, a + chunk)
+            if new:
+                u = torch.randint(spec.m, m_all, (b - a,), generator=gen, device=device).to(torch.int32)
+            else:
+                u = _draw(ucdf, urel, b - a, gen, device)
+            v = _draw(icdf, irel, b - a, gen, device)
+            r = spec.offset + spec.gain * (P[u.long()] * Q[v.long()]).sum(1)
+            r = r + torch.randn(b - a, generator=gen, device=device) * spec.noise_std
+            if spec.integer:
+                r = torch.round(r)
+            r = r.clamp_(spec.lo, spec.hi)
+            out["u"][a:b] = u.cpu().numpy()
+            out["v"][a:b] = v.cpu().numpy()
+            out["r"][a:b] = r.float().cpu().numpy()
+        return out
+
+    n_new = int(round(spec.nnz_train * new_frac))
+    new_test = int(round(n_new * test_frac / (1 - test_frac)))
+    return (block(spec.nnz_train, False), block(spec.nnz_test, False), block(n_new, True), block(new_test, True))

@@ -297,6 +297,40 @@ int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, i
 int cumf_tc_gemm(const void *d_A, const void *d_B, int M, int N, int K, const float *d_bias, int act,
                  void *d_out, int out_f32, int ldo, float *d_pre, int *d_status, void *stream);
 
+/* User features for the warm start, from ratings with ids already in [0,m) x [0,n) and fp32
+ * item factors Q (n x k): d_X (m x (k+3)) = [sum_i (r_ui - mean_u) q_i / deg_u,
+ * log(1+deg_u)/4, (mean_u - 3)/2, var_u/2]; users without ratings get zeros. */
+int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int32_t n, int k, int32_t m,
+                       float *d_X, void *stream);
+
+/* The warm-start MLP: d_in -> hidden (GELU) -> hidden (GELU) -> d_out, bf16 weights and
+ * activations with fp32 accumulation on the tensor cores, fp32 master weights, Adam.
+ * hidden and d_out must be multiples of 64.  The handle is opaque. */
+int cumf_mlp_create(int d_in, int hidden, int d_out, uint64_t seed, void **mlp);
+int cumf_mlp_destroy(void *mlp);
+/* Parameters flattened as W1[hidden][d_in], b1, W2[hidden][hidden], b2, W3[d_out][hidden], b3. */
+int64_t cumf_mlp_param_count(void *mlp);
+/* which = 0: parameters, 1: gradients of the last cumf_mlp_loss_grad / training step. */
+int cumf_mlp_get_params(void *mlp, float *host, int64_t count, int which);
+int cumf_mlp_set_params(void *mlp, const float *host, int64_t count);
+/* d_Y (rows x d_out, fp32) = MLP(d_X (rows x d_in, fp32)). */
+int cumf_mlp_forward(void *mlp, const float *d_X, int64_t rows, float *d_Y, void *stream);
+/* Mean-over-rows squared error against d_T and its gradients (kept in the handle). */
+int cumf_mlp_loss_grad(void *mlp, const float *d_X, const float *d_T, int64_t rows, double *loss, void *stream);
+/* Adam (0.9, 0.999) over shuffled mini-batches for `epochs` passes; *final_loss is the mean
+ * loss of the last pass. */
+int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, int epochs, int batch, float lr,
+                   uint64_t seed, double *final_loss, void *stream);
+
+/* cumf_train with a starting model and per-epoch evaluation (mode A only).  `init` (may be
+ * NULL) gives starting fp32 factors in the model file's layout for the first init->m users and
+ * init->n items (rows beyond them start from the usual random init); init->k must equal k.
+ * When `te` is given, epoch_rmse[e] receives the test RMSE after epoch e and epoch_ms[e] the
+ * cumulative training time (CUDA events, evaluation excluded); either may be NULL. */
+int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_params *params,
+                  const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
+                  double *epoch_ms);
+
 #ifdef __cplusplus
 }
 #endif

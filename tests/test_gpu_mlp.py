@@ -1,0 +1,73 @@
+"""Warm-start MLP on the tensor cores against its FP64 CPU restatement (oracle/mlp_oracle.py).
+Tolerances: activations and backward operands are bf16, so loss within 1% and each
+gradient tensor within 3% (relative L2) of FP64; features within 1e-4 relative (fp32 atomics)."""
+import numpy as np
+import pytest
+
+import cumf_sgd_gb300 as cm
+from oracle import mlp_oracle
+
+pytestmark = pytest.mark.gpu
+
+D_IN, H, D_OUT = 131, 512, 128
+
+
+def split(g):
+    return mlp_oracle.unpack(g, D_IN, H, D_OUT)
+
+
+@pytest.mark.parametrize("rows", [256, 300, 1000])
+def test_mlp_loss_and_gradients_match_fp64(lib, cuda, rows):
+    import torch
+    rng = np.random.default_rng(rows)
+    X = rng.standard_normal((rows, D_IN)).astype(np.float32) * 0.5
+    T = rng.standard_normal((rows, D_OUT)).astype(np.float32) * 0.2
+    mlp = cm.MLP(D_IN, H, D_OUT, seed=3)
+    params = mlp.get(0)
+    dX, dT = torch.from_numpy(X).to(cuda), torch.from_numpy(T).to(cuda)
+    loss = mlp.loss_grad(dX.data_ptr(), dT.data_ptr(), rows)
+    grads = mlp.get(1)
+    ref_loss, ref_grads = mlp_oracle.forward_backward(params, X, T, D_IN, H, D_OUT)
+    assert abs(loss - ref_loss) <= 0.01 * ref_loss, (loss, ref_loss)
+    for name, g, r in zip(["W1", "b1", "W2", "b2", "W3", "b3"], split(grads), split(ref_grads)):
+        err = np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-12)
+        assert err <= 0.03, (name, err)
+    Y = torch.empty(rows, D_OUT, device=cuda)
+    mlp.forward(dX.data_ptr(), rows, Y.data_ptr())
+    torch.cuda.synchronize()
+    W1, b1, W2, b2, W3, b3 = split(params)
+    ref_y = mlp_oracle.gelu(mlp_oracle.gelu(X @ W1.T + b1) @ W2.T + b2) @ W3.T + b3
+    assert np.linalg.norm(Y.cpu().numpy() - ref_y) <= 0.01 * np.linalg.norm(ref_y)
+
+
+def test_mlp_training_fits_a_smooth_map(lib, cuda):
+    import torch
+    rng = np.random.default_rng(0)
+    rows = 8192
+    X = rng.standard_normal((rows, D_IN)).astype(np.float32)
+    A = rng.standard_normal((D_IN, D_OUT)).astype(np.float32) / np.sqrt(D_IN)
+    T = np.tanh(X @ A).astype(np.float32)
+    mlp = cm.MLP(D_IN, H, D_OUT, seed=1)
+    dX, dT = torch.from_numpy(X).to(cuda), torch.from_numpy(T).to(cuda)
+    before = mlp.loss_grad(dX.data_ptr(), dT.data_ptr(), rows)
+    after = mlp.train(dX.data_ptr(), dT.data_ptr(), rows, epochs=20, batch=512, lr=1e-3, seed=2)
+    assert after < 0.1 * before, (before, after)
+
+
+def test_user_features_match_fp64(lib, cuda):
+    import torch
+    rng = np.random.default_rng(5)
+    m, n, k, nnz = 500, 200, 128, 20000
+    rec = np.empty(nnz, dtype=cm.NODE_DTYPE)
+    rec["u"] = rng.integers(0, m - 10, nnz)  # the last users have no ratings
+    rec["v"] = rng.integers(0, n, nnz)
+    rec["r"] = rng.integers(1, 6, nnz).astype(np.float32)
+    Q = (rng.standard_normal((n, k)) * 0.3).astype(np.float32)
+    dR = torch.from_numpy(rec.view(np.uint8).copy()).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    dX = torch.empty(m, k + 3, device=cuda)
+    cm.user_features(dR.data_ptr(), nnz, dQ.data_ptr(), n, k, m, dX.data_ptr())
+    got = dX.cpu().numpy()
+    ref = mlp_oracle.user_features(rec, Q, m, k)
+    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+    assert (got[-10:] == 0).all()
