@@ -364,6 +364,114 @@ def run_warmstart_suite(args):
              "speedup_vs_cold": (cold_ms / total) if (cold_ms and total) else None})
 
 
+def run_batched_suite(args):
+    """Batched factorizations (BASELINE config 4): 64 planted problems, users log-uniform in
+    [1k, 200k], items in [500, 20k], ratings in [50k, 10M], k in {32, 64, 128}, planted rank
+    in [8, 32], integer ratings 1..5, fp16 factors, 20 epochs.
+      sequential: per epoch, one plain update launch per problem (64 launches per epoch);
+      batched:    autotuned schedule, all 20 epochs of all 64 problems in one persistent
+                  launch captured in a CUDA graph.
+    Reports wall time (CUDA events) of each arm and the per-problem test RMSE of both."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+    build.build()
+    dev = torch.device("cuda", 0)
+    sm, _, _ = cm.device_info(0)
+    rng = np.random.default_rng(4)
+    nprob, epochs = 64, args.e2e_epochs
+    logu = lambda a, b: float(np.exp(rng.uniform(np.log(a), np.log(b))))
+    probs = []
+    t0 = time.time()
+    for i in range(nprob):
+        m, n = int(logu(1_000, 200_000)), int(logu(500, 20_000))
+        nnz = int(logu(50_000, 10_000_000) * args.scale)
+        k = int(rng.choice([32, 64, 128]))
+        spec = synth.PlantedSpec(m=m, n=n, nnz_train=nnz, nnz_test=max(1000, nnz // 9), rank=int(rng.integers(8, 33)),
+                                 user_s=0.5, item_s=0.5, factor_var=0.25, noise_std=0.5, offset=3.5, gain=1.0,
+                                 lo=1, hi=5, integer=True)
+        tr, te = synth.generate(spec, seed=1000 + i, device="cuda")
+        d_raw = torch.from_numpy(tr.view(np.uint8)).to(dev)
+        mean, std = cm.dev_rating_stats(d_raw.data_ptr(), nnz)
+        scale = max(np.float32(1e-4), np.float32(std))
+        pm = torch.from_numpy(cm.random_map(i, m)).to(dev)
+        qm = torch.from_numpy(cm.random_map(i, n)).to(dev)
+        d_R = torch.empty_like(d_raw)
+        cm.dev_shuffle_scale(d_raw.data_ptr(), d_R.data_ptr(), nnz, pm.data_ptr(), m, qm.data_ptr(), n,
+                             float(np.float32(1.0 / float(scale))))
+        P = torch.empty(m * k * 2, dtype=torch.uint8, device=dev)
+        Q = torch.empty(n * k * 2, dtype=torch.uint8, device=dev)
+        lr = torch.from_numpy(cm.lr_schedule(0.08, 0.3, 0.0, epochs + 4)).to(dev)
+        probs.append(dict(m=m, n=n, nnz=nnz, k=k, d_R=d_R, P=P, Q=Q, pm=pm, qm=qm, lr=lr, scale=scale,
+                          b=float(np.float32(mean) / np.float32(std)), lam=float(np.float32(0.05) / scale),
+                          te=torch.from_numpy(te.view(np.uint8)).to(dev), nte=len(te), seed=i))
+    print(json.dumps({"suite": "batched", "event": "generated", "problems": nprob,
+                      "total_nnz": sum(p["nnz"] for p in probs), "secs": time.time() - t0}), flush=True)
+
+    def init_all():
+        for p in probs:
+            cm.dev_init_factors(p["P"].data_ptr(), p["m"], p["k"], "fp16", p["seed"], 1)
+            cm.dev_init_factors(p["Q"].data_ptr(), p["n"], p["k"], "fp16", p["seed"], 2)
+        torch.cuda.synchronize()
+
+    def rmses():
+        out = []
+        for p in probs:
+            f = float(np.float32(np.sqrt(p["scale"])))
+            Pf = torch.empty(p["m"], p["k"], device=dev)
+            Qf = torch.empty(p["n"], p["k"], device=dev)
+            cm.dev_export_factors(p["P"].data_ptr(), "fp16", p["pm"].data_ptr(), p["m"], p["k"], f, Pf.data_ptr())
+            cm.dev_export_factors(p["Q"].data_ptr(), "fp16", p["qm"].data_ptr(), p["n"], p["k"], f, Qf.data_ptr())
+            out.append(cm.dev_rmse(p["te"].data_ptr(), p["nte"], Pf.data_ptr(), p["m"], Qf.data_ptr(), p["n"],
+                                   p["k"], p["b"]))
+        return np.array(out)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # sequential plain launches
+    init_all()
+    workers = [cm.auto_workers(p["nnz"], sm, p["k"], "fp16") for p in probs]
+    e0.record()
+    for e in range(epochs):
+        for p, w in zip(probs, workers):
+            cm.sgd_update(p["d_R"].data_ptr(), p["nnz"], p["P"].data_ptr(), p["m"], p["Q"].data_ptr(), p["n"],
+                          p["k"], "fp16", w, 0, p["lr"].data_ptr(), e, 1, p["lam"], p["lam"], p["seed"])
+    e1.record()
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    seq_rmse = rmses()
+    total = sum(p["nnz"] for p in probs)
+    print(json.dumps({"suite": "batched", "arm": "64 sequential plain launches per epoch", "epochs": epochs,
+                      "ms": seq_ms, "updates_per_sec": total * epochs / (seq_ms * 1e-3),
+                      "launches": epochs * nprob}), flush=True)
+    # batched persistent launch
+    init_all()
+    batch = cm.Batch([dict(d_R=p["d_R"].data_ptr(), nnz=p["nnz"], d_P=p["P"].data_ptr(), m=p["m"], n=p["n"],
+                           d_Q=p["Q"].data_ptr(), k=p["k"], lambda_p=p["lam"], lambda_q=p["lam"], seed=p["seed"],
+                           d_lr=p["lr"].data_ptr(), lr_len=epochs + 4) for p in probs])
+    t0 = time.time()
+    best = batch.autotune()
+    tune_s = time.time() - t0
+    batch.run(0, epochs, use_graph=True)  # capture + first replay happen here ...
+    torch.cuda.synchronize()
+    init_all()  # ... so start again from the same init for the timed replay
+    e0.record()
+    batch.run(0, epochs, use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    bat_ms = e0.elapsed_time(e1)
+    assert batch.status() == 0
+    bat_rmse = rmses()
+    info = batch.info()
+    print(json.dumps({"suite": "batched", "arm": "one graph-captured persistent launch", "epochs": epochs,
+                      "ms": bat_ms, "updates_per_sec": total * epochs / (bat_ms * 1e-3), "launches": 1,
+                      "tuning": best, "autotune_s": tune_s, "samples_per_epoch": info["samples_per_epoch"],
+                      "speedup_vs_sequential": seq_ms / bat_ms}), flush=True)
+    print(json.dumps({"suite": "batched", "event": "rmse", "sequential_mean": float(seq_rmse.mean()),
+                      "batched_mean": float(bat_rmse.mean()),
+                      "max_abs_diff": float(np.abs(seq_rmse - bat_rmse).max()),
+                      "per_problem": [[round(a, 4), round(b, 4)] for a, b in zip(seq_rmse, bat_rmse)]}), flush=True)
+
+
 def _has_cuda():
     try:
         import torch
@@ -388,7 +496,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
     ap.add_argument("--mlp-epochs", type=int, default=30)
     ap.add_argument("--warm-alpha", type=float, default=0.02, help="initial learning rate of warm refinement")
-    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart"],
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
     if args.suite == "precision":
@@ -396,6 +504,9 @@ def main():
         return
     if args.suite == "warmstart":
         run_warmstart_suite(args)
+        return
+    if args.suite == "batched":
+        run_batched_suite(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -438,3 +438,55 @@ def sgd_train_ex(tr: MFProblem, te: Optional[MFProblem], param: Parameter, init:
     _lib.check(rc)
     stats = TrainStats(**{f: getattr(st, f) for f, _ in _lib.TrainStats._fields_ if f != "reserved_"})
     return MFModel(out), stats, rm[:param.num_iters], ms[:param.num_iters]
+
+
+# ---- batched factorizations ------------------------------------------------------------
+
+class Batch:
+    """Many independent factorizations in one persistent launch (cumf_batch_* in the C ABI).
+    Each problem is a dict with device addresses d_R, d_P, d_Q, d_lr and m, n, nnz, k,
+    lambda_p, lambda_q, seed, lr_len and optionally num_workers."""
+
+    def __init__(self, problems):
+        arr = (_lib.BatchProblem * len(problems))()
+        for i, p in enumerate(problems):
+            arr[i] = _lib.BatchProblem(d_R=p["d_R"], nnz=p["nnz"], d_P=p["d_P"], m=p["m"], n=p["n"], d_Q=p["d_Q"],
+                                       k=p["k"], num_workers=p.get("num_workers", 0), lambda_p=p["lambda_p"],
+                                       lambda_q=p["lambda_q"], seed=p["seed"], d_lr=p["d_lr"], lr_len=p["lr_len"])
+        h = C.c_void_p()
+        _lib.check(_lib.load().cumf_batch_create(arr, len(problems), C.byref(h)))
+        self._h = h
+
+    def set_tuning(self, batches_target: int, order: int, blocks_per_sm: int) -> None:
+        t = _lib.BatchTuning(batches_target=batches_target, order=order, blocks_per_sm=blocks_per_sm)
+        _lib.check(_lib.load().cumf_batch_set_tuning(self._h, C.byref(t)))
+
+    def info(self):
+        t = _lib.BatchTuning()
+        tasks, samples = C.c_int(), C.c_int64()
+        _lib.check(_lib.load().cumf_batch_get_info(self._h, C.byref(t), C.byref(tasks), C.byref(samples)))
+        return dict(batches_target=t.batches_target, order=t.order, blocks_per_sm=t.blocks_per_sm,
+                    tasks_per_epoch=tasks.value, samples_per_epoch=samples.value)
+
+    def autotune(self, stream: int = 0):
+        t = _lib.BatchTuning()
+        ms = C.c_double()
+        _lib.check(_lib.load().cumf_batch_autotune(self._h, stream or None, C.byref(t), C.byref(ms)))
+        return dict(batches_target=t.batches_target, order=t.order, blocks_per_sm=t.blocks_per_sm,
+                    epoch_ms=ms.value)
+
+    def run(self, first_epoch: int, n_epochs: int, use_graph: bool = True, stream: int = 0) -> None:
+        _lib.check(_lib.load().cumf_batch_run(self._h, first_epoch, n_epochs, int(use_graph), stream or None))
+
+    def status(self) -> int:
+        st = C.c_int()
+        _lib.check(_lib.load().cumf_batch_status(self._h, C.byref(st)))
+        return st.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().cumf_batch_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

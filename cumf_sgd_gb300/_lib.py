@@ -67,6 +67,18 @@ class TrainStats(C.Structure):
                 ("reserved_", C.c_int32 * 5)]
 
 
+class BatchProblem(C.Structure):
+    _fields_ = [("d_R", C.c_void_p), ("nnz", C.c_int64), ("d_P", C.c_void_p), ("m", C.c_int32), ("n", C.c_int32),
+                ("d_Q", C.c_void_p), ("k", C.c_int32), ("num_workers", C.c_int32), ("lambda_p", C.c_float),
+                ("lambda_q", C.c_float), ("seed", C.c_uint64), ("d_lr", C.c_void_p), ("lr_len", C.c_int32),
+                ("reserved_", C.c_int32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("batches_target", C.c_int32), ("order", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("reserved_", C.c_int32 * 5)]
+
+
 class Args(C.Structure):
     _fields_ = [("param", Params), ("tr_path", C.c_char * 1024), ("va_path", C.c_char * 1024),
                 ("model_path", C.c_char * 1024)]
@@ -122,6 +134,13 @@ _SIGS = {
                                  C.POINTER(C.c_double), _VP]),
     "cumf_train_ex": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Model),
                                 C.POINTER(Model), C.POINTER(TrainStats), _VP, _VP]),
+    "cumf_batch_create": (C.c_int, [C.POINTER(BatchProblem), C.c_int, C.POINTER(C.c_void_p)]),
+    "cumf_batch_destroy": (C.c_int, [_VP]),
+    "cumf_batch_set_tuning": (C.c_int, [_VP, C.POINTER(BatchTuning)]),
+    "cumf_batch_get_info": (C.c_int, [_VP, C.POINTER(BatchTuning), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "cumf_batch_run": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _VP]),
+    "cumf_batch_status": (C.c_int, [_VP, C.POINTER(C.c_int)]),
+    "cumf_batch_autotune": (C.c_int, [_VP, _VP, C.POINTER(BatchTuning), C.POINTER(C.c_double)]),
     "cumf_device_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cumf_default_workers": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "cumf_auto_workers": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -33,6 +33,7 @@ LIB_SOURCES = [
     "noalloc.cu",
     "tc_gemm.cu",
     "mlp.cu",
+    "batch.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp"}
 

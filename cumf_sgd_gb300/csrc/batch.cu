@@ -1,0 +1,460 @@
+// batch.cu - many independent factorizations in one persistent launch.
+//
+// Problems of uneven size (m, n, nnz) and factor length k in {32, 64, 128}, fp16 factors,
+// share one launch: a grid of resident blocks whose 16-lane worker groups take tasks from a
+// global counter.  A task is one epoch of one Hogwild worker of one problem (its
+// ceil(nnz/(W*128)) batches of 128 records, exactly as in sgd_update.cu); the task table
+// lists an epoch's tasks in the order chosen by the autotuner, and epoch e+1's tasks follow
+// epoch e's in the counter (no barrier between epochs, as in the reference's persistent
+// kernel).  Each lane owns k/16 consecutive halves of a row (16, 8 or 4 bytes).
+// The launch (counter reset + kernel) can be captured in a CUDA graph and replayed.
+// Autotuning times candidate schedules (workers per problem, task order, blocks per SM)
+// with an all-zero learning-rate table: the kernel then does the same loads and stores but
+// writes back the values it read (p + 0 = p, exactly representable), so the factors are
+// left bit for bit unchanged.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "cumf_sgd.h"
+#include "device_common.cuh"
+#include "internal.h"
+#include "train_common.h"
+
+namespace cumf {
+
+namespace {
+
+constexpr int kBT = 256;       // threads per block
+constexpr int kBG = 16;        // lanes per worker
+constexpr int kBGPB = kBT / kBG;
+constexpr int kBChunk = 32;
+constexpr int kBWPL = kBChunk * 3 / kBG;
+
+struct BatchProblemDev {
+    const cumf_node *R;
+    uint64_t nnz;
+    void *P;
+    void *Q;
+    uint32_t m, n;
+    int k;
+    int workers;
+    int batches;
+    float lp, lq;
+    uint64_t seed;
+    const float *lr;
+};
+
+struct BatchTask {
+    int problem;
+    int worker;
+};
+
+template <int E>
+struct HalfVec;
+template <>
+struct HalfVec<8> {
+    using T = uint4;
+};
+template <>
+struct HalfVec<4> {
+    using T = uint2;
+};
+template <>
+struct HalfVec<2> {
+    using T = uint32_t;
+};
+
+template <typename T>
+__device__ __forceinline__ uint32_t &word(T &v, int w) {
+    return reinterpret_cast<uint32_t *>(&v)[w];
+}
+
+__device__ __forceinline__ void bcp_async4(void *smem, const void *gmem) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// One worker's epoch on one problem (16 lanes, E halves per lane).
+template <int E>
+__device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane, unsigned gmask,
+                         uint32_t (*s_rec)[3][kBChunk + 1], int *bad) {
+    using V = typename HalfVec<E>::T;
+    constexpr int W = E / 2;  // 32-bit words (half pairs) per lane
+    const int K = E * kBG;
+    V *const P = reinterpret_cast<V *>(pr.P) + lane;
+    V *const Q = reinterpret_cast<V *>(pr.Q) + lane;
+    const uint32_t *const Rw = reinterpret_cast<const uint32_t *>(pr.R);
+    const uint64_t nnz = pr.nnz;
+    const float lr = __ldg(pr.lr + ep);
+    const int chunks = pr.batches * (128 / kBChunk);
+    const int rowv = K * 2 / (int)sizeof(V);  // V words per row
+    (void)rowv;
+    auto fetch = [&](int t, int buf) {
+        const uint64_t start = batch_start(pr.seed, ep, worker, t / (128 / kBChunk), nnz);
+        uint64_t base = start + (uint64_t)((t % (128 / kBChunk)) * kBChunk);
+        while (base >= nnz) base -= nnz;
+#pragma unroll
+        for (int i = 0; i < kBWPL; ++i) {
+            const int w = lane + i * kBG;
+            uint64_t rec = base + (uint64_t)(w / 3);
+            while (rec >= nnz) rec -= nnz;
+            bcp_async4(&s_rec[buf][w % 3][w / 3], Rw + rec * 3 + (w % 3));
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    fetch(0, 0);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncwarp(gmask);
+    uint32_t u = s_rec[0][0][0], v = s_rec[0][1][0];
+    bool ok = (u < pr.m) & (v < pr.n);
+    V fp = ok ? __ldcg(P + (uint64_t)u * kBG) : V{};
+    V fq = ok ? __ldcg(Q + (uint64_t)v * kBG) : V{};
+    for (int t = 0; t < chunks; ++t) {
+        const int buf = t & 1;
+        const bool has_next = t + 1 < chunks;
+        if (has_next) fetch(t + 1, buf ^ 1);
+#pragma unroll 1
+        for (int j = 0; j < kBChunk; ++j) {
+            uint32_t un = 0xffffffffu, vn = 0xffffffffu;
+            if (j + 1 < kBChunk) {
+                un = s_rec[buf][0][j + 1];
+                vn = s_rec[buf][1][j + 1];
+            } else if (has_next) {
+                asm volatile("cp.async.wait_all;\n" ::: "memory");
+                __syncwarp(gmask);
+                un = s_rec[buf ^ 1][0][0];
+                vn = s_rec[buf ^ 1][1][0];
+            }
+            const bool okn = (un < pr.m) & (vn < pr.n);
+            V np = okn ? __ldcg(P + (uint64_t)un * kBG) : V{};
+            V nq = okn ? __ldcg(Q + (uint64_t)vn * kBG) : V{};
+            if (ok) {
+                const float r = __uint_as_float(s_rec[buf][2][j]);
+                float s = 0.f;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp, w)));
+                    const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq, w)));
+                    s = __fmaf_rn(pp.x, qq.x, s);
+                    s = __fmaf_rn(pp.y, qq.y, s);
+                }
+#pragma unroll
+                for (int o = kBG / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                const float err = r - s;
+                V wp, wq;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp, w)));
+                    const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq, w)));
+                    const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(pr.lp, pp.x)), pp.x);
+                    const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(pr.lp, pp.y)), pp.y);
+                    const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(pr.lq, qq.x)), qq.x);
+                    const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(pr.lq, qq.y)), qq.y);
+                    __half2 hp = __floats2half2_rn(px, py), hq = __floats2half2_rn(qx, qy);
+                    word(wp, w) = *reinterpret_cast<uint32_t *>(&hp);
+                    word(wq, w) = *reinterpret_cast<uint32_t *>(&hq);
+                }
+                __stcg(P + (uint64_t)u * kBG, wp);
+                __stcg(Q + (uint64_t)v * kBG, wq);
+                if (un == u) np = wp;
+                if (vn == v) nq = wq;
+            } else {
+                *bad = 1;
+            }
+            fp = np;
+            fq = nq;
+            u = un;
+            v = vn;
+            ok = okn;
+        }
+        __syncwarp(gmask);
+    }
+}
+
+__global__ void __launch_bounds__(kBT, 4)
+batch_kernel(const BatchProblemDev *probs, const BatchTask *tasks, int tasks_per_epoch, int first_epoch, int n_epochs,
+             int *counter, int *status) {
+    __shared__ uint32_t s_rec[kBGPB][2][3][kBChunk + 1];
+    const int lane = threadIdx.x % kBG;
+    const int gib = threadIdx.x / kBG;
+    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(kBG - 1));
+    const int leader = (threadIdx.x & 31) & ~(kBG - 1);
+    const long long total = (long long)tasks_per_epoch * n_epochs;
+    int bad = 0;
+    while (true) {
+        long long g = 0;
+        if (lane == 0) g = atomicAdd(counter, 1);
+        g = __shfl_sync(gmask, g, leader);
+        if (g >= total) break;
+        const int ep = first_epoch + (int)(g / tasks_per_epoch);
+        const BatchTask t = tasks[g % tasks_per_epoch];
+        const BatchProblemDev pr = probs[t.problem];
+        if (pr.nnz == 0 || pr.batches == 0) continue;
+        switch (pr.k) {
+            case 128: run_task<8>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+            case 64: run_task<4>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+            case 32: run_task<2>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+            default: bad = 1; break;
+        }
+    }
+    if (bad && status && lane == 0) atomicExch(status, (int)CUMF_ERR_RANGE);
+}
+
+}  // namespace
+
+struct Batch {
+    std::vector<cumf_batch_problem> probs;
+    std::vector<BatchProblemDev> dev_probs;
+    cumf_batch_tuning tuning;
+    DevBuf d_probs, d_probs_zero_lr, d_tasks, d_counter, d_status, d_zero_lr;
+    int tasks_per_epoch = 0;
+    int sm_count = 0;
+    int64_t samples_per_epoch = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_first = -1, graph_n = -1;
+    ~Batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+namespace {
+
+int64_t work_of(const cumf_batch_problem &p) { return p.nnz * (int64_t)p.k; }
+
+// Rebuilds worker counts, the device problem table and the task table for b->tuning.
+int batch_plan(Batch *b) {
+    const cumf_batch_tuning &t = b->tuning;
+    const int nprob = (int)b->probs.size();
+    b->dev_probs.resize(nprob);
+    b->samples_per_epoch = 0;
+    std::vector<int> workers(nprob);
+    for (int i = 0; i < nprob; ++i) {
+        const cumf_batch_problem &p = b->probs[i];
+        int w = p.num_workers;
+        if (w <= 0) {  // enough workers for ~batches_target batches each
+            const int64_t target = std::max(1, t.batches_target);
+            w = (int)std::max<int64_t>(1, (p.nnz + 128 * target - 1) / (128 * target));
+        }
+        workers[i] = w;
+        BatchProblemDev &d = b->dev_probs[i];
+        d.R = p.d_R;
+        d.nnz = (uint64_t)p.nnz;
+        d.P = p.d_P;
+        d.Q = p.d_Q;
+        d.m = (uint32_t)p.m;
+        d.n = (uint32_t)p.n;
+        d.k = p.k;
+        d.workers = w;
+        d.batches = (int)batches_per_worker(p.nnz, w);
+        d.lp = p.lambda_p;
+        d.lq = p.lambda_q;
+        d.seed = p.seed;
+        d.lr = p.d_lr;
+        b->samples_per_epoch += (int64_t)w * d.batches * 128;
+    }
+    std::vector<int> order(nprob);
+    std::iota(order.begin(), order.end(), 0);
+    if (t.order == 2)  // largest problems first
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int c) { return work_of(b->probs[a]) > work_of(b->probs[c]); });
+    std::vector<BatchTask> tasks;
+    if (t.order == 1) {  // round robin across problems
+        int maxw = 0;
+        for (int i : order) maxw = std::max(maxw, workers[i]);
+        for (int w = 0; w < maxw; ++w)
+            for (int i : order)
+                if (w < workers[i]) tasks.push_back({i, w});
+    } else {
+        for (int i : order)
+            for (int w = 0; w < workers[i]; ++w) tasks.push_back({i, w});
+    }
+    b->tasks_per_epoch = (int)tasks.size();
+    CUMF_CUDA(b->d_probs.alloc(std::max<size_t>(1, nprob) * sizeof(BatchProblemDev)));
+    CUMF_CUDA(cudaMemcpy(b->d_probs.p, b->dev_probs.data(), nprob * sizeof(BatchProblemDev), cudaMemcpyHostToDevice));
+    std::vector<BatchProblemDev> zl = b->dev_probs;
+    for (BatchProblemDev &d : zl) d.lr = b->d_zero_lr.as<float>();
+    CUMF_CUDA(b->d_probs_zero_lr.alloc(std::max<size_t>(1, nprob) * sizeof(BatchProblemDev)));
+    CUMF_CUDA(cudaMemcpy(b->d_probs_zero_lr.p, zl.data(), nprob * sizeof(BatchProblemDev), cudaMemcpyHostToDevice));
+    CUMF_CUDA(b->d_tasks.alloc(std::max<size_t>(1, tasks.size()) * sizeof(BatchTask)));
+    CUMF_CUDA(cudaMemcpy(b->d_tasks.p, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice));
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_first = b->graph_n = -1;
+    return CUMF_OK;
+}
+
+cudaError_t batch_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const int bps = std::max(1, std::min(4, b->tuning.blocks_per_sm));
+    batch_kernel<<<bps * b->sm_count, kBT, 0, s>>>(
+        zero_lr ? b->d_probs_zero_lr.as<BatchProblemDev>() : b->d_probs.as<BatchProblemDev>(),
+        b->d_tasks.as<BatchTask>(), b->tasks_per_epoch, first_epoch, n_epochs, b->d_counter.as<int>(),
+        b->d_status.as<int>());
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+}  // namespace cumf
+
+using namespace cumf;
+
+extern "C" {
+
+int cumf_batch_create(const cumf_batch_problem *probs, int count, void **handle) {
+    if (!probs || count <= 0 || !handle) return fail(CUMF_ERR_ARG, "batch_create: bad arguments");
+    int max_epoch_index = 0;
+    for (int i = 0; i < count; ++i) {
+        const cumf_batch_problem &p = probs[i];
+        if (p.k != 32 && p.k != 64 && p.k != 128)
+            return fail(CUMF_ERR_ARG, "batch_create: k must be 32, 64 or 128 (problem " + std::to_string(i) + ")");
+        if (p.nnz < 0 || p.m < 1 || p.n < 1 || (p.nnz > 0 && (!p.d_R || !p.d_P || !p.d_Q || !p.d_lr)))
+            return fail(CUMF_ERR_ARG, "batch_create: malformed problem " + std::to_string(i));
+        if (p.num_workers > 0 && batches_per_worker(p.nnz, p.num_workers) * 4 > 0x7fffffffll)
+            return fail(CUMF_ERR_ARG, "batch_create: too many batches per worker");
+        max_epoch_index = std::max(max_epoch_index, p.lr_len);
+    }
+    Batch *b = new Batch();
+    b->probs.assign(probs, probs + count);
+    b->tuning.batches_target = 16;
+    b->tuning.order = 2;
+    b->tuning.blocks_per_sm = 4;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    auto bail = [&](int rc) {
+        delete b;
+        return rc;
+    };
+    if (cudaError_t e = b->d_counter.alloc(sizeof(int))) return bail(cuda_fail(e, "batch counter"));
+    if (cudaError_t e = b->d_status.alloc(sizeof(int))) return bail(cuda_fail(e, "batch status"));
+    if (cudaError_t e = b->d_zero_lr.alloc(std::max(1, max_epoch_index) * sizeof(float)))
+        return bail(cuda_fail(e, "batch zero lr"));
+    cudaMemset(b->d_status.p, 0, sizeof(int));
+    cudaMemset(b->d_zero_lr.p, 0, std::max(1, max_epoch_index) * sizeof(float));
+    if (int rc = batch_plan(b)) return bail(rc);
+    *handle = b;
+    return CUMF_OK;
+}
+
+int cumf_batch_destroy(void *handle) {
+    delete static_cast<Batch *>(handle);
+    return CUMF_OK;
+}
+
+int cumf_batch_set_tuning(void *handle, const cumf_batch_tuning *t) {
+    Batch *b = static_cast<Batch *>(handle);
+    if (!b || !t || t->order < 0 || t->order > 2 || t->batches_target < 1 || t->blocks_per_sm < 1 ||
+        t->blocks_per_sm > 4)
+        return fail(CUMF_ERR_ARG, "batch_set_tuning: bad tuning");
+    b->tuning = *t;
+    return batch_plan(b);
+}
+
+int cumf_batch_get_info(void *handle, cumf_batch_tuning *t, int *tasks_per_epoch, int64_t *samples_per_epoch) {
+    Batch *b = static_cast<Batch *>(handle);
+    if (!b) return fail(CUMF_ERR_ARG, "batch_get_info: NULL handle");
+    if (t) *t = b->tuning;
+    if (tasks_per_epoch) *tasks_per_epoch = b->tasks_per_epoch;
+    if (samples_per_epoch) *samples_per_epoch = b->samples_per_epoch;
+    return CUMF_OK;
+}
+
+int cumf_batch_run(void *handle, int first_epoch, int n_epochs, int use_graph, void *stream) {
+    Batch *b = static_cast<Batch *>(handle);
+    if (!b || first_epoch < 0 || n_epochs < 0) return fail(CUMF_ERR_ARG, "batch_run: bad arguments");
+    for (const cumf_batch_problem &p : b->probs)
+        if (first_epoch + n_epochs > p.lr_len) return fail(CUMF_ERR_ARG, "batch_run: epochs beyond a problem's lr table");
+    if (n_epochs == 0) return CUMF_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!use_graph) {
+        CUMF_CUDA(batch_launch(b, false, first_epoch, n_epochs, s));
+        return CUMF_OK;
+    }
+    if (!b->exec || b->graph_first != first_epoch || b->graph_n != n_epochs) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        cudaStream_t cap;
+        CUMF_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = batch_launch(b, false, first_epoch, n_epochs, cap);
+        cudaError_t e2 = cudaStreamEndCapture(cap, &b->graph);
+        cudaStreamDestroy(cap);
+        if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "batch graph end capture");
+        CUMF_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        b->graph_first = first_epoch;
+        b->graph_n = n_epochs;
+    }
+    CUMF_CUDA(cudaGraphLaunch(b->exec, s));
+    return CUMF_OK;
+}
+
+int cumf_batch_status(void *handle, int *status) {
+    Batch *b = static_cast<Batch *>(handle);
+    if (!b || !status) return fail(CUMF_ERR_ARG, "batch_status: bad arguments");
+    CUMF_CUDA(cudaMemcpy(status, b->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    return CUMF_OK;
+}
+
+int cumf_batch_autotune(void *handle, void *stream, cumf_batch_tuning *best, double *best_ms) {
+    Batch *b = static_cast<Batch *>(handle);
+    if (!b) return fail(CUMF_ERR_ARG, "batch_autotune: NULL handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    Event e0, e1;
+    CUMF_CUDA(e0.create());
+    CUMF_CUDA(e1.create());
+    cumf_batch_tuning cand, top = b->tuning;
+    double top_ms = 1e30;
+    memset(&cand, 0, sizeof(cand));
+    const int targets[] = {4, 8, 16, 32};
+    const int orders[] = {0, 1, 2};
+    const int occ[] = {3, 4};
+    for (int bt : targets)
+        for (int o : orders)
+            for (int bps : occ) {
+                cand.batches_target = bt;
+                cand.order = o;
+                cand.blocks_per_sm = bps;
+                b->tuning = cand;
+                if (int rc = batch_plan(b)) return rc;
+                CUMF_CUDA(batch_launch(b, true, 0, 1, s));  // warm-up, zero learning rate
+                CUMF_CUDA(cudaEventRecord(e0.e, s));
+                CUMF_CUDA(batch_launch(b, true, 0, 1, s));
+                CUMF_CUDA(cudaEventRecord(e1.e, s));
+                CUMF_CUDA(cudaEventSynchronize(e1.e));
+                float ms = 0;
+                CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
+                // time per sample, so schedules with different budgets compare fairly
+                const double per = ms / (double)std::max<int64_t>(1, b->samples_per_epoch);
+                if (per < top_ms) {
+                    top_ms = per;
+                    top = cand;
+                }
+            }
+    b->tuning = top;
+    if (int rc = batch_plan(b)) return rc;
+    if (best) *best = top;
+    if (best_ms) *best_ms = top_ms * (double)b->samples_per_epoch;
+    return CUMF_OK;
+}
+
+}  // extern "C"

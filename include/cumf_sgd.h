@@ -331,6 +331,52 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
                   const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
                   double *epoch_ms);
 
+/* ---- batched factorizations (no reference counterpart) ------------------------------ */
+/* One problem of a batch: device ratings with ids in range and ratings already scaled, fp16
+ * factors P (m x k) and Q (n x k), k in {32, 64, 128}; num_workers 0 = set by the batch
+ * tuning; d_lr has lr_len learning rates (epoch index < lr_len). */
+typedef struct cumf_batch_problem {
+    const cumf_node *d_R;
+    int64_t nnz;
+    void *d_P;
+    int32_t m;
+    int32_t n;
+    void *d_Q;
+    int32_t k;
+    int32_t num_workers;
+    float lambda_p, lambda_q;
+    uint64_t seed;
+    const float *d_lr;
+    int32_t lr_len;
+    int32_t reserved_;
+} cumf_batch_problem;
+
+/* Schedule of a batched launch: workers per problem so each has about batches_target
+ * 128-record batches per epoch (problems with num_workers > 0 keep theirs); task order
+ * 0 = problem by problem, 1 = round robin over problems, 2 = largest problems first;
+ * blocks_per_sm 1..4 of the persistent grid. */
+typedef struct cumf_batch_tuning {
+    int32_t batches_target;
+    int32_t order;
+    int32_t blocks_per_sm;
+    int32_t reserved_[5];
+} cumf_batch_tuning;
+
+/* Copies the problem descriptors (the device buffers stay the caller's). */
+int cumf_batch_create(const cumf_batch_problem *probs, int count, void **batch);
+int cumf_batch_destroy(void *batch);
+int cumf_batch_set_tuning(void *batch, const cumf_batch_tuning *tuning);
+int cumf_batch_get_info(void *batch, cumf_batch_tuning *tuning, int *tasks_per_epoch, int64_t *samples_per_epoch);
+/* Epochs [first_epoch, first_epoch + n_epochs) of every problem in one persistent launch;
+ * use_graph = 1 captures the launch (counter reset + kernel) in a CUDA graph on first use and
+ * replays it while (first_epoch, n_epochs) and the tuning stay the same. */
+int cumf_batch_run(void *batch, int first_epoch, int n_epochs, int use_graph, void *stream);
+/* CUMF_ERR_RANGE if any launch met an out-of-range index (such ratings are skipped). */
+int cumf_batch_status(void *batch, int *status);
+/* Times every candidate schedule for one epoch with a zero learning rate (factors are left
+ * bit for bit unchanged), keeps the fastest per sample and returns it. */
+int cumf_batch_autotune(void *batch, void *stream, cumf_batch_tuning *best, double *best_epoch_ms);
+
 #ifdef __cplusplus
 }
 #endif
