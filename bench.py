@@ -195,8 +195,8 @@ def run_precision_suite(args):
     if not args.no_e2e:
         prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n, pinned=True)
         tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+        W = cm.auto_workers(len(train), sm, K, "fp32")  # one worker count for every storage type
         for prec in precs:
-            W = cm.auto_workers(len(train), sm, K, prec)
             par = cm.Parameter(k=K, num_workers=W, num_iters=epochs, alpha=0.08, beta=0.3, seed=1, gpu=0,
                                precision=prec)
             model, st = cm.sgd_train(prob, None, par, with_stats=True)

@@ -2,11 +2,11 @@
 //
 // Problems of uneven size (m, n, nnz) and factor length k in {32, 64, 128}, fp16 factors,
 // share one launch: a grid of resident blocks whose 16-lane worker groups take tasks from a
-// global counter.  A task is one epoch of one Hogwild worker of one problem (its
-// ceil(nnz/(W*128)) batches of 128 records, exactly as in sgd_update.cu); the task table
-// lists an epoch's tasks in the order chosen by the autotuner, and epoch e+1's tasks follow
-// epoch e's in the counter (no barrier between epochs, as in the reference's persistent
-// kernel).  Each lane owns k/16 consecutive halves of a row (16, 8 or 4 bytes).
+// global counter.  A task is one Hogwild worker of one problem: it runs that worker's
+// epochs of the launch in order, each its ceil(nnz/(W*128)) batches of 128 records exactly as
+// in sgd_update.cu, so a problem never has more than W workers in flight and there is no
+// barrier between epochs (as in the reference's persistent kernel).  The task table order is
+// chosen by the autotuner.  Each lane owns k/16 consecutive halves of a row (16, 8 or 4 B).
 // The launch (counter reset + kernel) can be captured in a CUDA graph and replayed.
 // Autotuning times candidate schedules (workers per problem, task order, blocks per SM)
 // with an all-zero learning-rate table: the kernel then does the same loads and stores but
@@ -87,15 +87,12 @@ __device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane
                          uint32_t (*s_rec)[3][kBChunk + 1], int *bad) {
     using V = typename HalfVec<E>::T;
     constexpr int W = E / 2;  // 32-bit words (half pairs) per lane
-    const int K = E * kBG;
     V *const P = reinterpret_cast<V *>(pr.P) + lane;
     V *const Q = reinterpret_cast<V *>(pr.Q) + lane;
     const uint32_t *const Rw = reinterpret_cast<const uint32_t *>(pr.R);
     const uint64_t nnz = pr.nnz;
     const float lr = __ldg(pr.lr + ep);
     const int chunks = pr.batches * (128 / kBChunk);
-    const int rowv = K * 2 / (int)sizeof(V);  // V words per row
-    (void)rowv;
     auto fetch = [&](int t, int buf) {
         const uint64_t start = batch_start(pr.seed, ep, worker, t / (128 / kBChunk), nnz);
         uint64_t base = start + (uint64_t)((t % (128 / kBChunk)) * kBChunk);
@@ -186,22 +183,22 @@ batch_kernel(const BatchProblemDev *probs, const BatchTask *tasks, int tasks_per
     const int gib = threadIdx.x / kBG;
     const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(kBG - 1));
     const int leader = (threadIdx.x & 31) & ~(kBG - 1);
-    const long long total = (long long)tasks_per_epoch * n_epochs;
     int bad = 0;
     while (true) {
-        long long g = 0;
+        int g = 0;
         if (lane == 0) g = atomicAdd(counter, 1);
         g = __shfl_sync(gmask, g, leader);
-        if (g >= total) break;
-        const int ep = first_epoch + (int)(g / tasks_per_epoch);
-        const BatchTask t = tasks[g % tasks_per_epoch];
+        if (g >= tasks_per_epoch) break;
+        const BatchTask t = tasks[g];
         const BatchProblemDev pr = probs[t.problem];
         if (pr.nnz == 0 || pr.batches == 0) continue;
-        switch (pr.k) {
-            case 128: run_task<8>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-            case 64: run_task<4>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-            case 32: run_task<2>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-            default: bad = 1; break;
+        for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
+            switch (pr.k) {
+                case 128: run_task<8>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+                case 64: run_task<4>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+                case 32: run_task<2>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
+                default: bad = 1; break;
+            }
         }
     }
     if (bad && status && lane == 0) atomicExch(status, (int)CUMF_ERR_RANGE);
