@@ -290,7 +290,8 @@ def run_warmstart_suite(args):
     X = torch.cat(Xs).contiguous()
     T = torch.cat(Ts).contiguous()
     mlp = cm.MLP(K + 3, 512, K, seed=7)
-    loss0 = mlp.loss_grad(X.data_ptr(), T.data_ptr(), len(X))
+    probe = min(len(X), 65536)
+    loss0 = mlp.loss_grad(X.data_ptr(), T.data_ptr(), probe)
     torch.cuda.synchronize()
     t1 = time.time()
     loss = mlp.train(X.data_ptr(), T.data_ptr(), len(X), epochs=args.mlp_epochs, batch=4096 if big else 1024,
@@ -472,6 +473,42 @@ def run_batched_suite(args):
                       "per_problem": [[round(a, 4), round(b, 4)] for a, b in zip(seq_rmse, bat_rmse)]}), flush=True)
 
 
+def run_gemm_suite(args):
+    """tcgen05 BF16 GEMM (the MLP's products) on its training shapes: TFLOP/s from CUDA-event
+    time over repeated launches, against the measured dense bf16 peak (MEASURED_PEAKS.json)."""
+    import torch
+    from cumf_sgd_gb300 import build, _lib
+    build.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    peak = 1955.0
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        peak = float(json.load(open(path))["bf16_tflops"])
+    rows = int(65536 * args.scale)
+    shapes = [("fwd layer 1", rows, 512, 192), ("fwd layer 2", rows, 512, 512), ("fwd layer 3", rows, 128, 512),
+              ("dX layer 2", rows, 512, 512), ("dW layer 2", 512, 512, rows), ("dW layer 1", 512, 192, rows)]
+    for name, M, N, K in shapes:
+        A = (torch.randn(M, K, device=dev) * 0.5).to(torch.bfloat16)
+        B = (torch.randn(N, K, device=dev) * 0.5).to(torch.bfloat16)
+        out = torch.empty(M, N, device=dev)
+        for _ in range(3):
+            assert lib.cumf_tc_gemm(A.data_ptr(), B.data_ptr(), M, N, K, None, 0, out.data_ptr(), 1, N, None, None,
+                                    None) == 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = args.steps
+        e0.record()
+        for _ in range(reps):
+            lib.cumf_tc_gemm(A.data_ptr(), B.data_ptr(), M, N, K, None, 0, out.data_ptr(), 1, N, None, None, None)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        tf = 2.0 * M * N * K / (ms * 1e-3) / 1e12
+        err = (out - A.float() @ B.float().T).abs().max().item()
+        print(json.dumps({"suite": "gemm", "shape": name, "M": M, "N": N, "K": K, "ms": ms, "tflops": tf,
+                          "peak_tflops": peak, "frac": tf / peak, "max_abs_err_vs_fp32": err}), flush=True)
+
+
 def _has_cuda():
     try:
         import torch
@@ -496,7 +533,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
     ap.add_argument("--mlp-epochs", type=int, default=30)
     ap.add_argument("--warm-alpha", type=float, default=0.02, help="initial learning rate of warm refinement")
-    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched"],
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
     if args.suite == "precision":
@@ -507,6 +544,9 @@ def main():
         return
     if args.suite == "batched":
         run_batched_suite(args)
+        return
+    if args.suite == "gemm":
+        run_gemm_suite(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -94,9 +94,10 @@ __global__ void to_bf16_pad_kernel(const float *S, int64_t rows, int cols, int l
 }
 
 // D[c][r] = S[r][c] for a rows x cols bf16 matrix (tiled through shared memory).
+// Row tiles run along gridDim.x (up to 2^31 - 1), column tiles along gridDim.y.
 __global__ void transpose_bf16_kernel(const __nv_bfloat16 *S, int rows, int cols, __nv_bfloat16 *D) {
     __shared__ __nv_bfloat16 tile[32][33];
-    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    const int bx = blockIdx.y * 32, by = blockIdx.x * 32;
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const int r = by + j, c = bx + threadIdx.x;
         tile[j][threadIdx.x] = (r < rows && c < cols) ? S[(int64_t)r * cols + c] : __float2bfloat16_rn(0.f);
@@ -228,7 +229,8 @@ int mlp_ensure(Mlp *mp, int64_t rows) {
 }
 
 cudaError_t transpose(const void *S, int rows, int cols, void *D, cudaStream_t s) {
-    dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+    dim3 grid((rows + 31) / 32, (cols + 31) / 32), block(32, 8);
+    if (grid.y > 65535) return cudaErrorInvalidValue;
     transpose_bf16_kernel<<<grid, block, 0, s>>>(reinterpret_cast<const __nv_bfloat16 *>(S), rows, cols,
                                                   reinterpret_cast<__nv_bfloat16 *>(D));
     return cudaGetLastError();
