@@ -231,22 +231,24 @@ def run_precision_suite(args):
 
 
 def run_warmstart_suite(args):
-    """Learned warm start (BASELINE config 5, and the c2-shape headline with --scale-c2).
+    """Learned warm start (BASELINE config 5; with --scale 2 the c2-shape headline).
 
-    Scenario: a deployed model exists for a base matrix; 50,000 new users arrive with ratings
-    amounting to 5% of the base train count (one planted model for all users, seeded).
-      1. MLP training data: 8 plain-SGD solves (fp16, 20 epochs) of c1-shaped planted
-         matrices with different seeds; per user, features from (ratings, solved Q), target
-         the solved P row.  The MLP trains on the tensor cores (cumf_mlp_train).
-      2. Base model: plain fp16 SGD on the base matrix (not timed: it is the deployed model).
-      3. Target: the serial FP64 oracle trained from scratch on the grown matrix for 20
-         epochs; target = its test RMSE + 0.002.
-      4. Cold start: plain fp16 SGD from random init on the grown matrix.
-         Warm start: base P for old users, MLP(features) for new users, base Q; bf16 with
-         stochastic rounding; time includes feature extraction and MLP inference.
-         Ablation: the same warm start with random new-user rows (no MLP).
+    Scenario: a deployed model exists for a base matrix (c1 or c2 shape); 50,000 new users
+    arrive with ratings amounting to 5% of the base train count (one planted model for all).
+      1. MLP training data: 8 plain-SGD solves (fp16, 20 epochs) of planted matrices of the
+         same family with other seeds; per user, features from (ratings, solved Q), target the
+         solved P row.  The MLP trains on the tensor cores (cumf_mlp_train).
+      2. Base model: plain fp16 SGD on the base matrix (not timed: the deployed model, kept
+         in device memory).
+      3. Target: the FP64 oracle trained from scratch on the grown matrix for 20 epochs (serial
+         at c1 shape; at c2 shape its batches run on all host cores) + 0.002.
+      4. Cold start: plain fp16 SGD from random init on the grown matrix (up to 40 epochs).
+         Warm start: base P for old users, MLP(features) for new users, base Q, refined with the
+         given storage and initial learning rate, the first epochs over the new users' ratings
+         only (the tail of the rating array); its time includes feature extraction and MLP
+         inference on device-resident data.  Ablation: random rows for new users (no MLP).
     Time-to-target = cumulative CUDA-event training time up to the first epoch whose test
-    RMSE <= target (evaluation excluded), plus the warm start's own preparation time."""
+    RMSE <= target (evaluation excluded) + the warm start's preparation time."""
     import torch
     import cumf_sgd_gb300 as cm
     from cumf_sgd_gb300 import synth, build
@@ -258,22 +260,20 @@ def run_warmstart_suite(args):
     big = args.scale >= 2.0
     base_spec = synth.C2 if big else synth.C1
     new_users = 50_000
-    epochs = args.e2e_epochs
     out = lambda d: print(json.dumps({"suite": "warmstart", "shape": "c2" if big else "c1", **d}), flush=True)
 
-    def solve(tr, m, n, seed, precision="fp16", iters=20, init=None, te=None, alpha=0.08):
+    def solve(tr, m, n, seed, precision="fp16", iters=20, init=None, te=None, alpha=0.08, tail_epochs=0,
+              tail_start=0, beta=0.3):
         prob = cm.MFProblem.from_arrays(tr["u"], tr["v"], tr["r"], m=m, n=n)
         tprob = cm.MFProblem.from_arrays(te["u"], te["v"], te["r"]) if te is not None else None
         W = cm.auto_workers(len(tr), sm, K, precision)
-        par = cm.Parameter(k=K, num_workers=W, num_iters=iters, alpha=alpha, beta=0.3, seed=seed, gpu=0,
-                           precision=precision)
+        par = cm.Parameter(k=K, num_workers=W, num_iters=iters, alpha=alpha, beta=beta, seed=seed, gpu=0,
+                           precision=precision, tail_epochs=tail_epochs, tail_start=tail_start)
         return cm.sgd_train_ex(prob, tprob, par, init)
 
-    def features(tr, m, n, Q):
-        dR = torch.from_numpy(tr.view(np.uint8).copy()).to(dev)
-        dQ = torch.from_numpy(np.ascontiguousarray(Q)).to(dev)
+    def features(dR, nnz, m, n, dQ):
         dX = torch.empty(m, K + 3, device=dev)
-        cm.user_features(dR.data_ptr(), len(tr), dQ.data_ptr(), n, K, m, dX.data_ptr())
+        cm.user_features(dR.data_ptr(), nnz, dQ.data_ptr(), n, K, m, dX.data_ptr())
         return dX
 
     # 1. MLP training data from 8 solves of the same family
@@ -282,9 +282,9 @@ def run_warmstart_suite(args):
     for s in range(8):
         tr, _ = synth.generate(base_spec, seed=10 + s, device="cuda")
         model, _, _, _ = solve(tr, base_spec.m, base_spec.n, seed=10 + s)
-        X = features(tr, base_spec.m, base_spec.n, model.Q)
-        deg = np.bincount(tr["u"], minlength=base_spec.m)
-        keep = torch.from_numpy(np.nonzero(deg > 0)[0]).to(dev)
+        dR = torch.from_numpy(tr.view(np.uint8).copy()).to(dev)
+        X = features(dR, len(tr), base_spec.m, base_spec.n, torch.from_numpy(np.ascontiguousarray(model.Q)).to(dev))
+        keep = torch.from_numpy(np.nonzero(np.bincount(tr["u"], minlength=base_spec.m) > 0)[0]).to(dev)
         Xs.append(X[keep])
         Ts.append(torch.from_numpy(np.ascontiguousarray(model.P)).to(dev)[keep])
     X = torch.cat(Xs).contiguous()
@@ -299,70 +299,82 @@ def run_warmstart_suite(args):
     torch.cuda.synchronize()
     out({"event": "mlp_trained", "rows": len(X), "loss_before": loss0, "loss_after": loss,
          "train_s": time.time() - t1, "data_s": t1 - t0})
+    del X, T, Xs, Ts
 
-    # 2. base + growth from one planted model
+    # 2. base + growth from one planted model; the deployed base model lives on the device
     b_tr, b_te, n_tr, n_te = synth.generate_growth(base_spec, new_users, 0.05, seed=100, device="cuda")
     m_all, n = base_spec.m + new_users, base_spec.n
     base_model, _, _, _ = solve(b_tr, base_spec.m, n, seed=1)
+    base_P = torch.from_numpy(np.ascontiguousarray(base_model.P)).to(dev)
+    base_Q = torch.from_numpy(np.ascontiguousarray(base_model.Q)).to(dev)
     g_tr = np.concatenate([b_tr, n_tr])
     g_te = np.concatenate([b_te, n_te])
+    d_gtr = torch.from_numpy(g_tr.view(np.uint8).copy()).to(dev)
     out({"event": "data", "base_train": len(b_tr), "new_train": len(n_tr), "test": len(g_te),
          "new_test": len(n_te), "users": m_all, "items": n})
 
-    # 3. FP64 oracle target (c1 shape; at c2 shape the target is cold fp16's 20-epoch RMSE)
-    if not big:
-        t0 = time.time()
-        W = cm.auto_workers(len(g_tr), sm, K, "fp16")
-        P64, Q64, b64 = oracle.train_f64(g_tr, m_all, n, k=K, num_workers=W, num_iters=20, seed=5)
-        oracle_rmse = oracle.calc_rmse_f64(g_te, P64, Q64, b64)
-        target = oracle_rmse + 0.002
-        out({"event": "oracle", "fp64_test_rmse": oracle_rmse, "target": target, "secs": time.time() - t0})
+    # 3. FP64 target
+    t0 = time.time()
+    W = cm.auto_workers(len(g_tr), sm, K, "fp16")
+    threads = 1 if not big else (os.cpu_count() or 1)
+    P64, Q64, b64 = oracle.train_f64(g_tr, m_all, n, k=K, num_workers=W, num_iters=20, seed=5, threads=threads)
+    oracle_rmse = oracle.calc_rmse_f64(g_te, P64, Q64, b64)
+    target = oracle_rmse + 0.002
+    out({"event": "oracle", "fp64_test_rmse": oracle_rmse, "target": target, "host_threads": threads,
+         "secs": time.time() - t0})
+    del P64, Q64
 
-    def time_to_target(rm, ms, target):
+    def time_to_target(rm, ms):
         for e in range(len(rm)):
             if rm[e] <= target:
                 return float(ms[e]), e + 1
         return None, None
 
     # 4. cold start
-    _, cst, crm, cms = solve(g_tr, m_all, n, seed=5, precision="fp16", iters=epochs, te=g_te)
-    if big:
-        target = float(crm[-1]) + 0.002
-        out({"event": "target", "definition": "cold fp16 RMSE after %d epochs + 0.002" % epochs, "target": target})
-    cold_ms, cold_ep = time_to_target(crm, cms, target)
+    _, _, crm, cms = solve(g_tr, m_all, n, seed=5, precision="fp16", iters=40, te=g_te)
+    cold_ms, cold_ep = time_to_target(crm, cms)
     out({"arm": "cold fp16", "epoch_rmse": [round(x, 5) for x in crm], "epoch_ms": [round(x, 3) for x in cms],
          "time_to_target_ms": cold_ms, "epochs_to_target": cold_ep})
 
-    # warm start: features + MLP inference for every user (timed), base rows for old users
-    def warm(use_mlp):
+    def warm(use_mlp, precision, alpha, beta, tail_epochs):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        P0 = np.zeros((m_all, K), dtype=np.float32)
-        P0[: base_spec.m] = base_model.P
-        if use_mlp:
-            Xg = features(g_tr, m_all, n, base_model.Q)
-            Y = torch.empty(m_all, K, device=dev)
-            mlp.forward(Xg.data_ptr(), m_all, Y.data_ptr())
-            P0[base_spec.m:] = Y[base_spec.m:].cpu().numpy()
+        P0 = torch.empty(m_all, K, device=dev)
+        P0[: base_spec.m] = base_P
+        if use_mlp:  # features from the new users' ratings only (the tail of the array)
+            tail = d_gtr[len(b_tr) * 12:]
+            Xg = features(tail, len(n_tr), m_all, n, base_Q)
+            Xn = Xg[base_spec.m:].contiguous()
+            Y = torch.empty(new_users, K, device=dev)
+            mlp.forward(Xn.data_ptr(), new_users, Y.data_ptr())
+            P0[base_spec.m:] = Y
         else:
-            P0[base_spec.m:] = oracle.init_factors(new_users, K, "fp32", 9, 1)
-        init = cm.MFModel.from_arrays(P0, base_model.Q, base_model.b)
+            P0[base_spec.m:] = torch.from_numpy(oracle.init_factors(new_users, K, "fp32", 9, 1)).to(dev)
+        torch.cuda.synchronize()
         prep_ms = (time.perf_counter() - t0) * 1e3
-        _, wst, wrm, wms = solve(g_tr, m_all, n, seed=5, precision="bf16sr", iters=epochs, init=init, te=g_te,
-                                 alpha=args.warm_alpha)
-        new_prob = cm.MFProblem.from_arrays(n_te["u"], n_te["v"], n_te["r"])
-        init_rmse_new = cm.calc_rmse(new_prob, init)
+        init = cm.DeviceModel(P0.data_ptr(), m_all, base_Q.data_ptr(), n, K)
+        _, _, wrm, wms = solve(g_tr, m_all, n, seed=5, precision=precision, iters=args.e2e_epochs, init=init,
+                               te=g_te, alpha=alpha, beta=beta, tail_epochs=tail_epochs, tail_start=len(b_tr))
+        Pn = P0[base_spec.m:].contiguous()
+        d_nte = torch.from_numpy((n_te.copy()).view(np.uint8)).to(dev)
+        d_nte_view = d_nte.view(torch.int32).view(-1, 3)
+        d_nte_view[:, 0] -= base_spec.m
+        init_rmse_new = cm.dev_rmse(d_nte.data_ptr(), len(n_te), Pn.data_ptr(), new_users, base_Q.data_ptr(), n, K,
+                                    float(base_model.b))
         return prep_ms, wrm, wms, init_rmse_new
 
+    configs = [c.split(":") for c in args.warm_configs.split(",")]
     for use_mlp in (True, False):
-        prep_ms, wrm, wms, init_new = warm(use_mlp)
-        w_ms, w_ep = time_to_target(wrm, wms, target)
-        total = None if w_ms is None else w_ms + prep_ms
-        out({"arm": "warm bf16sr" + ("" if use_mlp else " (no MLP: random new users)"),
-             "prep_ms": prep_ms, "new_user_test_rmse_at_init": init_new,
-             "epoch_rmse": [round(x, 5) for x in wrm], "epoch_ms": [round(x, 3) for x in wms],
-             "time_to_target_ms": total, "epochs_to_target": w_ep,
-             "speedup_vs_cold": (cold_ms / total) if (cold_ms and total) else None})
+        for precision, alpha, beta, tail in (configs if use_mlp else configs[:1]):
+            prep_ms, wrm, wms, init_new = warm(use_mlp, precision, float(alpha), float(beta), int(tail))
+            w_ms, w_ep = time_to_target(wrm, wms)
+            total = None if w_ms is None else w_ms + prep_ms
+            out({"arm": f"warm {precision} alpha={alpha} beta={beta} new-user epochs={tail}" +
+                        ("" if use_mlp else " (no MLP: random new users)"),
+                 "prep_ms": prep_ms, "new_user_test_rmse_at_init": init_new,
+                 "epoch_rmse": [round(x, 5) for x in wrm], "epoch_ms": [round(x, 3) for x in wms],
+                 "time_to_target_ms": total, "epochs_to_target": w_ep,
+                 "speedup_vs_cold": (cold_ms / total) if (cold_ms and total) else None})
 
 
 def run_batched_suite(args):
@@ -532,7 +544,9 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
     ap.add_argument("--mlp-epochs", type=int, default=30)
-    ap.add_argument("--warm-alpha", type=float, default=0.02, help="initial learning rate of warm refinement")
+    ap.add_argument("--warm-configs",
+                    default="bf16sr:0.04:0.3:4,bf16sr:0.02:0.05:8,bf16sr:0.04:0.3:2,fp16:0.04:0.3:4,bf16sr:0.02:0.3:0",
+                    help="warm-start refinements as storage:alpha:beta:new_user_epochs, comma separated")
     ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()

@@ -52,6 +52,8 @@ class Parameter:
     prefetch: int = -1
     l2_hints: int = -1
     ring: int = -1
+    tail_epochs: int = 0
+    tail_start: int = 0
 
     @property
     def ux(self) -> int:
@@ -66,7 +68,7 @@ class Parameter:
         _lib.check(_lib.load().cumf_default_params(C.byref(p)))
         for f in ("k", "num_workers", "u_grid", "v_grid", "x_grid", "y_grid", "num_iters", "gpu",
                   "lambda_p", "lambda_q", "lrate", "alpha", "beta", "seed", "lanes",
-                  "epochs_per_launch", "prefetch", "l2_hints", "ring"):
+                  "epochs_per_launch", "prefetch", "l2_hints", "ring", "tail_epochs", "tail_start"):
             setattr(p, f, getattr(self, f))
         p.precision = PRECISIONS[self.precision] if isinstance(self.precision, str) else int(self.precision)
         p.quiet = int(bool(self.quiet))
@@ -327,9 +329,10 @@ def auto_workers(nnz: int, sm_count: int, k: int, precision: str = "fp16", lanes
 def sgd_update(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, precision: str,
                num_workers: int, lanes: int, d_lr: int, first_epoch: int, n_epochs: int,
                lambda_p: float, lambda_q: float, seed: int, d_status: int = 0,
-               stream: int = 0, prefetch: int = -1, l2_hints: int = -1, ring: int = -1) -> None:
+               stream: int = 0, prefetch: int = -1, l2_hints: int = -1, ring: int = -1,
+               freeze_q: int = 0) -> None:
     """Batch-Hogwild epochs on caller-owned device buffers (sgd_kernel.cu:212-248)."""
-    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints, ring=ring)
+    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints, ring=ring, freeze_q=freeze_q)
     _lib.check(_lib.load().cumf_sgd_update_tuned(d_R, nnz, d_P, m, d_Q, n, k, PRECISIONS[precision],
                                                  num_workers, C.byref(t), d_lr, first_epoch, n_epochs,
                                                  lambda_p, lambda_q, seed, d_status or None,
@@ -424,7 +427,16 @@ def user_features(d_R: int, nnz: int, d_Q: int, n: int, k: int, m: int, d_X: int
     _lib.check(_lib.load().cumf_user_features(d_R, nnz, d_Q, n, k, m, d_X, stream or None))
 
 
-def sgd_train_ex(tr: MFProblem, te: Optional[MFProblem], param: Parameter, init: Optional[MFModel] = None):
+class DeviceModel:
+    """A starting model whose fp32 factors live in device memory (not owned): P (m x k) and
+    Q (n x k) given as device addresses, for sgd_train_ex."""
+
+    def __init__(self, d_P: int, m: int, d_Q: int, n: int, k: int, b: float = 0.0):
+        self._c = _lib.Model(fun=0, m=m, n=n, k=k, b=b, pinned=2, P=C.cast(C.c_void_p(d_P), C.POINTER(C.c_float)),
+                             Q=C.cast(C.c_void_p(d_Q), C.POINTER(C.c_float)))
+
+
+def sgd_train_ex(tr: MFProblem, te: Optional[MFProblem], param: Parameter, init=None):
     """sgd_train with optional starting factors and per-epoch test RMSE; returns
     (model, stats, epoch_rmse, epoch_cumulative_train_ms)."""
     out = _lib.Model()

@@ -45,12 +45,13 @@ class Params(C.Structure):
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("lanes", C.c_int32),
                 ("quiet", C.c_int32), ("epochs_per_launch", C.c_int32),
                 ("verbose_epochs", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("ring", C.c_int32), ("reserved_", C.c_int32 * 2)]
+                ("ring", C.c_int32), ("tail_epochs", C.c_int32), ("reserved_", C.c_int32),
+                ("tail_start", C.c_int64)]
 
 
 class Tuning(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("ring", C.c_int32), ("reserved_", C.c_int32 * 4)]
+                ("ring", C.c_int32), ("freeze_q", C.c_int32), ("reserved_", C.c_int32 * 3)]
 
 
 class Model(C.Structure):

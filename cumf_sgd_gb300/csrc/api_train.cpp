@@ -130,13 +130,23 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         const int64_t mi = std::min<int64_t>(init->m, m), ni = std::min<int64_t>(init->n, n);
         DevBuf tmp;
         CUMF_CUDA(tmp.alloc((size_t)std::max(mi, ni) * k * sizeof(float)));
+        const bool on_device = init->pinned == 2;  // P and Q are device addresses
         if (mi > 0) {
-            CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->P, (size_t)mi * k * sizeof(float), cudaMemcpyHostToDevice, s));
-            CUMF_CUDA(launch_import(tmp.as<float>(), d_pmap.as<int32_t>(), mi, k, f0, d_P.p, p.precision, s));
+            const float *src = init->P;
+            if (!on_device) {
+                CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->P, (size_t)mi * k * sizeof(float), cudaMemcpyHostToDevice, s));
+                src = tmp.as<float>();
+            }
+            CUMF_CUDA(launch_import(src, d_pmap.as<int32_t>(), mi, k, f0, d_P.p, p.precision, s));
         }
         if (ni > 0) {
-            CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->Q, (size_t)ni * k * sizeof(float), cudaMemcpyHostToDevice, s));
-            CUMF_CUDA(launch_import(tmp.as<float>(), d_qmap.as<int32_t>(), ni, k, f0, d_Q.p, p.precision, s));
+            CUMF_CUDA(cudaStreamSynchronize(s));  // tmp is reused
+            const float *src = init->Q;
+            if (!on_device) {
+                CUMF_CUDA(cudaMemcpyAsync(tmp.p, init->Q, (size_t)ni * k * sizeof(float), cudaMemcpyHostToDevice, s));
+                src = tmp.as<float>();
+            }
+            CUMF_CUDA(launch_import(src, d_qmap.as<int32_t>(), ni, k, f0, d_Q.p, p.precision, s));
         }
         CUMF_CUDA(cudaStreamSynchronize(s));
     }
@@ -169,17 +179,30 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(cudaGetDevice(&dev));
     CUMF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const bool one_wave = workers <= resident_workers(k, p.precision, lanes, sms);
-    const int per_launch = (per_epoch || !one_wave) ? 1
+    const int per_launch = (per_epoch || !one_wave || p.tail_epochs > 0) ? 1
                            : (p.epochs_per_launch > 0 ? p.epochs_per_launch : std::max(1, p.num_iters));
+    const bool tail = p.tail_epochs > 0 && p.tail_start > 0 && p.tail_start < nnz;
     for (int ep = 0; ep < p.num_iters; ep += per_launch) {
-        const int cnt = std::min(per_launch, p.num_iters - ep);
+        int cnt = std::min(per_launch, p.num_iters - ep);
+        const cumf_node *R_ep = d_R.as<cumf_node>();
+        int64_t nnz_ep = nnz;
+        int workers_ep = workers;
+        if (tail && ep < p.tail_epochs) {  // epochs over the tail of the rating array only,
+            cnt = 1;                        // with at most one worker per 1024 of its ratings
+            R_ep += p.tail_start;
+            nnz_ep = nnz - p.tail_start;
+            workers_ep = (int)std::min<int64_t>(workers, std::max<int64_t>(1, nnz_ep / 1024));
+        } else if (tail) {
+            cnt = std::min(cnt, p.num_iters - ep);
+        }
         CUMF_CUDA(cudaEventRecord(e0.e, s));
         Tuning tu;
         tu.lanes = lanes;
         tu.prefetch = p.prefetch;
         tu.hints = p.l2_hints;
         tu.ring = p.ring;
-        CUMF_CUDA(launch_sgd_update(d_R.as<cumf_node>(), nnz, d_P.p, m, d_Q.p, n, k, p.precision, workers, tu,
+        tu.freeze_q = (tail && ep < p.tail_epochs) ? 1 : 0;  // fold-in: items stay as given
+        CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m, d_Q.p, n, k, p.precision, workers_ep, tu,
                                     d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
                                     &lanes_used));
         CUMF_CUDA(cudaEventRecord(e1.e, s));
@@ -390,6 +413,7 @@ int cumf_sgd_update_tuned(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t 
         tu.prefetch = tuning->prefetch;
         tu.hints = tuning->l2_hints;
         tu.ring = tuning->ring;
+        tu.freeze_q = tuning->freeze_q;
     }
     const int lanes = tu.lanes;
     if (nnz < 0 || num_workers < 1 || first_epoch < 0 || n_epochs < 0 || m < 1 || n < 1)

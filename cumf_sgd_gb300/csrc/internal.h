@@ -33,6 +33,7 @@ struct Tuning {
     int prefetch = -1;  // -1 = default
     int hints = -1;     // -1 = default
     int ring = -1;      // -1 = default, 0 = register prefetch kernel, 1 = shared-memory ring kernel
+    int freeze_q = 0;   // 1 = item rows are not written
 };
 Tuning resolve_tuning(int k, int precision, Tuning t);
 int default_lanes(int k, int precision);

@@ -4,6 +4,8 @@
 // Features of user u (k + 3 values), from the user's ratings and the item factors Q:
 //   x[0:k] = sum_i (r_ui - mean_u) q_i / deg_u      (rating-centred mean of the rated items)
 //   x[k]   = log(1 + deg_u) / 4,  x[k+1] = (mean_u - 3) / 2,  x[k+2] = var_u / 2
+// The centred mean is zero for a user with one rating, so users with few ratings stay inside
+// the range the network was trained on (an uncentred mean of one item's factors does not).
 // MLP: d_in -> H (GELU) -> H (GELU) -> d_out, bf16 weights and activations, fp32
 // accumulation (tcgen05), fp32 master weights updated with Adam.  Every matrix product of the
 // forward and backward passes is a TN product C = A B^T on the tcgen05 GEMM:
@@ -51,7 +53,7 @@ __global__ void user_stats_kernel(const cumf_node *R, int64_t nnz, int32_t m, in
     }
 }
 
-// One warp per rating: feature[u][0:k] += (r - mean_u) * q_v / deg_u.
+// One warp per rating: acc[u][0:k] += (r - mean_u) q_v / deg_u.
 __global__ void user_qsum_kernel(const cumf_node *R, int64_t nnz, int32_t m, int32_t n, const float *Q, int k,
                                  const float *deg, const float *sum, float *X, int ldx) {
     const int lane = threadIdx.x & 31;
@@ -64,7 +66,16 @@ __global__ void user_qsum_kernel(const cumf_node *R, int64_t nnz, int32_t m, int
         const float c = (x.r - sum[x.u] / d) / d;
         const float *q = Q + (int64_t)x.v * k;
         float *dst = X + (int64_t)x.u * ldx;
-        for (int j = lane; j < k; j += 32) atomicAdd(dst + j, c * q[j]);
+        if ((k & 3) == 0 && (ldx & 3) == 0) {  // 16-byte vector atomics (sm_90+)
+            const float4 *q4 = reinterpret_cast<const float4 *>(q);
+            float4 *d4 = reinterpret_cast<float4 *>(dst);
+            for (int j = lane; j < (k >> 2); j += 32) {
+                const float4 a = q4[j];
+                atomicAdd(d4 + j, make_float4(c * a.x, c * a.y, c * a.z, c * a.w));
+            }
+        } else {
+            for (int j = lane; j < k; j += 32) atomicAdd(dst + j, c * q[j]);
+        }
     }
 }
 
@@ -484,14 +495,20 @@ int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int3
     CUMF_CUDA(cudaMemsetAsync(deg.p, 0, (size_t)m * 4, s));
     CUMF_CUDA(cudaMemsetAsync(sum.p, 0, (size_t)m * 4, s));
     CUMF_CUDA(cudaMemsetAsync(sum2.p, 0, (size_t)m * 4, s));
+    // The centred mean accumulates in a k-wide buffer (16-byte aligned rows for the vector
+    // atomics), then lands in the (k+3)-wide feature rows beside the scalar features.
     const int ldx = k + 3;
-    CUMF_CUDA(cudaMemsetAsync(d_X, 0, (size_t)m * ldx * 4, s));
+    DevBuf acc;
+    CUMF_CUDA(acc.alloc((size_t)m * k * 4));
+    CUMF_CUDA(cudaMemsetAsync(acc.p, 0, (size_t)m * k * 4, s));
     if (nnz > 0) {
         user_stats_kernel<<<grid_of(nnz), kT, 0, s>>>(d_R, nnz, m, n, deg.as<float>(), sum.as<float>(),
                                                        sum2.as<float>());
         user_qsum_kernel<<<grid_of(nnz * 32), kT, 0, s>>>(d_R, nnz, m, n, d_Q, k, deg.as<float>(), sum.as<float>(),
-                                                           d_X, ldx);
+                                                           acc.as<float>(), k);
     }
+    CUMF_CUDA(cudaMemcpy2DAsync(d_X, (size_t)ldx * 4, acc.p, (size_t)k * 4, (size_t)k * 4, m,
+                                cudaMemcpyDeviceToDevice, s));
     user_scalar_kernel<<<grid_of(m), kT, 0, s>>>(m, k, deg.as<float>(), sum.as<float>(), sum2.as<float>(), d_X, ldx);
     CUMF_CUDA(cudaGetLastError());
     CUMF_CUDA(cudaStreamSynchronize(s));

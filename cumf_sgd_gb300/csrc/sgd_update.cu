@@ -53,6 +53,7 @@ struct UpdateArgs {
     int *status;
     int prefetch;   // rows of record j+prefetch are pulled into L2 while record j runs (0 = off)
     int hints;      // 1 = L2 eviction hints (ratings evict_first, factor rows evict_last)
+    int freeze_q;   // 1 = item rows are read but never written (user-side fold-in)
 };
 
 // Copy of a word the compiler cannot see through: the update phase re-widens the packed
@@ -230,10 +231,14 @@ sgd_hogwild_kernel(const UpdateArgs a) {
                             }
                         }
                     }
+                    if (a.freeze_q) {
+#pragma unroll
+                        for (int i = 0; i < NV; ++i) wq[i] = fq[i];
+                    }
 #pragma unroll
                     for (int i = 0; i < NV; ++i) {
                         st_row_hint(P + (uint64_t)u * ROW_WORDS + i, wp[i], pol_row);
-                        st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
+                        if (!a.freeze_q) st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
                     }
                     // Forward the fresh rows when the next record reuses them (its loads
                     // were issued before these stores).
@@ -446,10 +451,14 @@ sgd_ring_kernel(const UpdateArgs a) {
                         }
                     }
                 }
+                if (a.freeze_q) {
+#pragma unroll
+                    for (int i = 0; i < NV; ++i) wq[i] = fq[i];
+                }
 #pragma unroll
                 for (int i = 0; i < NV; ++i) {
                     st_row_hint(P + (uint64_t)u * ROW_WORDS + i, wp[i], pol_row);
-                    st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
+                    if (!a.freeze_q) st_row_hint(Q + (uint64_t)v * ROW_WORDS + i, wq[i], pol_row);
                 }
             } else {
                 bad = 1;
@@ -598,6 +607,7 @@ cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int3
     a.status = d_status;
     a.prefetch = t.prefetch;
     a.hints = t.hints;
+    a.freeze_q = t.freeze_q;
     const int gpb = kBlock / e->lanes;
     const int blocks = (num_workers + gpb - 1) / gpb;
     if (t.ring) {

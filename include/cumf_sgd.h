@@ -99,7 +99,9 @@ typedef struct cumf_params {
     int32_t prefetch;      /* L2 prefetch distance in records: -1 = tuned default, 0 = off */
     int32_t l2_hints;      /* L2 eviction hints: -1 = tuned default, 0 = off, 1 = on      */
     int32_t ring;          /* update kernel pipeline (see cumf_tuning.ring)               */
-    int32_t reserved_[2];
+    int32_t tail_epochs;   /* the first tail_epochs epochs sample only records            */
+    int32_t reserved_;     /*   [tail_start, nnz) (e.g. newly added users' ratings) and     */
+    int64_t tail_start;    /*   update user rows only (item rows frozen), then all records */
 } cumf_params;
 
 /* Launch tuning of the update kernel (the knobs the autotuner searches). */
@@ -112,7 +114,8 @@ typedef struct cumf_tuning {
     int32_t ring;          /* -1 = default, 0 = one record's rows in flight per worker (held
                               in registers), 1 = four records' rows in flight, staged by
                               cp.async in a shared-memory ring                            */
-    int32_t reserved_[4];
+    int32_t freeze_q;      /* 1 = update user rows only; item rows are read, never written  */
+    int32_t reserved_[3];
 } cumf_tuning;
 
 /* mf_model (singleGPU/sgd.h:110-138) as the model file holds it (main.cpp:247-266):
@@ -325,6 +328,7 @@ int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, 
 /* cumf_train with a starting model and per-epoch evaluation (mode A only).  `init` (may be
  * NULL) gives starting fp32 factors in the model file's layout for the first init->m users and
  * init->n items (rows beyond them start from the usual random init); init->k must equal k.
+ * init->pinned == 2 marks init->P and init->Q as device addresses (no host copy).
  * When `te` is given, epoch_rmse[e] receives the test RMSE after epoch e and epoch_ms[e] the
  * cumulative training time (CUDA events, evaluation excluded); either may be NULL. */
 int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_params *params,

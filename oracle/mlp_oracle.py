@@ -56,7 +56,8 @@ def forward_backward(params, X, T, d_in, h, d_out):
 
 
 def user_features(records, Q, m, k):
-    """Features of users 0..m-1 (see cumf_user_features), float64."""
+    """Features of users 0..m-1 (see cumf_user_features): rating-centred mean of the rated
+    items' factors, log-degree, rating mean and variance; float64."""
     u = records["u"].astype(np.int64)
     v = records["v"].astype(np.int64)
     r = records["r"].astype(np.float64)

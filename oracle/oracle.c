@@ -580,3 +580,35 @@ double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t 
     }
     return sqrt(loss / (double)nnz);
 }
+
+typedef struct {
+    or_sgd64_args *a;
+    int tid, threads;
+} f64_thread_arg;
+
+static void *f64_thread(void *p) {
+    f64_thread_arg *t = (f64_thread_arg *)p;
+    or_sgd64_args *a = t->a;
+    const int64_t per = (int64_t)a->num_workers * 128;
+    const int64_t batches = (a->nnz + per - 1) / per;
+    for (int ep = a->first_epoch; ep < a->first_epoch + a->n_epochs; ep++)
+        for (int64_t b = 0; b < batches; b++)
+            for (int w = t->tid; w < a->num_workers; w += t->threads) run_batch_f64(a, ep, w, b, a->lr[ep]);
+    return NULL;
+}
+
+void or_sgd_epochs_f64_threads(or_sgd64_args *a, int threads) {
+    if (a->nnz <= 0 || a->num_workers <= 0) return;
+    if (threads < 1) threads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    f64_thread_arg *args = (f64_thread_arg *)malloc(sizeof(f64_thread_arg) * threads);
+    for (int t = 0; t < threads; t++) {
+        args[t].a = a;
+        args[t].tid = t;
+        args[t].threads = threads;
+        pthread_create(&th[t], NULL, f64_thread, &args[t]);
+    }
+    for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+    free(th);
+    free(args);
+}

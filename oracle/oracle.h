@@ -144,6 +144,8 @@ typedef struct or_sgd64_args {
 void or_sgd_epochs_f64(or_sgd64_args *a);
 /* FP64 factor init: U(0,1] * sqrt(1/k) in double with the same uniforms as or_init_factors. */
 void or_init_factors_f64(double *out, int64_t rows, int k, uint64_t seed, uint32_t tag);
+/* The FP64 trainer's batches dealt to `threads` POSIX threads (Hogwild on the host). */
+void or_sgd_epochs_f64_threads(or_sgd64_args *a, int threads);
 /* RMSE of an FP64 model (double dot and error). */
 double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t m, const double *Q,
                         int32_t n, int k, double b);

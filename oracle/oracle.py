@@ -116,6 +116,7 @@ def lib() -> C.CDLL:
         _lib.or_shuffle_model.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int]
         _lib.or_scale_model.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_float]
         _lib.or_sgd_epochs_f64.argtypes = [C.POINTER(_Sgd64Args)]
+        _lib.or_sgd_epochs_f64_threads.argtypes = [C.POINTER(_Sgd64Args), C.c_int]
         _lib.or_init_factors_f64.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_uint32]
         _lib.or_calc_rmse_f64.restype = C.c_double
         _lib.or_calc_rmse_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
@@ -271,9 +272,10 @@ def ref_rmse(test_path: str, model_path: str) -> float:
 
 def train_f64(records: np.ndarray, m: int, n: int, k: int = 128, num_workers: int = 1, num_iters: int = 20,
               lambda_p: float = 0.05, lambda_q: float = 0.05, alpha: float = 0.08, beta: float = 0.3,
-              lrate: float = 0.0, seed: int = 0, order: int = OR_ORDER_ROUND_ROBIN):
-    """Serial FP64 sgd_train (mode A): the same statistics, id maps, sample schedule and
-    learning-rate table as the GPU path, everything else in double.  Returns (P, Q, b) with
+              lrate: float = 0.0, seed: int = 0, order: int = OR_ORDER_ROUND_ROBIN, threads: int = 1):
+    """FP64 sgd_train (mode A): the same statistics, id maps, sample schedule and
+    learning-rate table as the GPU path, everything else in double; serial when threads == 1,
+    else the workers' batches are dealt to `threads` host threads.  Returns (P, Q, b) with
     float64 factors (unscaled, un-permuted)."""
     rec = np.ascontiguousarray(records).copy()
     ave, std = collect_data(rec)
@@ -288,7 +290,10 @@ def train_f64(records: np.ndarray, m: int, n: int, k: int = 128, num_workers: in
     a = _Sgd64Args(R=_ptr(rec), nnz=len(rec), P=_ptr(P), m=m, Q=_ptr(Q), n=n, k=k, num_workers=num_workers,
                    order=order, lr=_ptr(lr), first_epoch=0, n_epochs=num_iters, lambda_p=lambda_p / scale,
                    lambda_q=lambda_q / scale, rscale=1.0 / scale, seed=seed)
-    lib().or_sgd_epochs_f64(C.byref(a))
+    if threads > 1:
+        lib().or_sgd_epochs_f64_threads(C.byref(a), threads)
+    else:
+        lib().or_sgd_epochs_f64(C.byref(a))
     f = np.sqrt(scale)
     return P[pm] * f, Q[qm] * f, float(ave) / float(std)
 

@@ -330,3 +330,23 @@ def test_streamed_mode_hogwild_converges_like_mode_a(lib, cuda):
     rb = cm.calc_rmse(test, cm.sgd_train(prob, None, cm.Parameter(**base, u_grid=2, v_grid=2)))
     rc = cm.calc_rmse(test, cm.sgd_train(prob, None, cm.Parameter(**base, u_grid=2, v_grid=2, x_grid=2, y_grid=2)))
     assert abs(rb - ra) < 0.02 and abs(rc - ra) < 0.02, (ra, rb, rc)
+
+
+@pytest.mark.parametrize("ring", [0, 1], ids=["regs", "ring"])
+def test_freeze_q_updates_users_only(lib, orc, cuda, ring):
+    """Fold-in epochs: item rows are left bit for bit as given, user rows move."""
+    import torch
+    m, n, k = 50, 30, 128
+    rec = small_problem(m, n, 4000, 77)
+    d_R = dev(rec, cuda)
+    P = torch.empty(m * k * 2, dtype=torch.uint8, device=cuda)
+    Q = torch.empty(n * k * 2, dtype=torch.uint8, device=cuda)
+    cm.dev_init_factors(P.data_ptr(), m, k, "fp16", 5, 1)
+    cm.dev_init_factors(Q.data_ptr(), n, k, "fp16", 5, 2)
+    P0, Q0 = P.clone(), Q.clone()
+    lr = torch.from_numpy(orc.lr_table(0.08, 0.3, 0.0, 4)).to(cuda)
+    cm.sgd_update(d_R.data_ptr(), len(rec), P.data_ptr(), m, Q.data_ptr(), n, k, "fp16", 8, 0, lr.data_ptr(), 0, 2,
+                  0.05, 0.05, 5, ring=ring, freeze_q=1)
+    torch.cuda.synchronize()
+    assert torch.equal(Q, Q0)
+    assert not torch.equal(P, P0)
