@@ -8,7 +8,10 @@ ratings, k = 128, fp16 factors, 20 epochs, synthetic (seeded) in place of Netfli
          out, 20 epochs including H2D, prep, export and D2H);
   roofline   algorithmic bytes of the update kernel (12 + 4k bytes per sample) / launch time
              against the measured HBM copy bandwidth;
-  cpu_baseline  the oracle's threaded CPU port of the same algorithm (fp32) on the host cores.
+  cpu_baseline  the oracle's threaded CPU port of the same algorithm (fp32) on the host cores;
+  time_to_target  the second half of the metric: c2-shape growth scenario, cold fp16 SGD
+             against the learned warm start with bf16 stochastic rounding (see
+             run_warmstart_suite), time to reach the FP64 oracle's test RMSE + 0.002.
 `--impl reference` times that CPU port alone as the reference arm (the reference's own
 binaries are x86 builds of this container and do not exist on the GPU host).
 Multi-GPU (torchrun): independent replicas, one per GPU (weak scaling, no collective).
@@ -230,7 +233,7 @@ def run_precision_suite(args):
                           "test_rmse": r, "gap_to_fp64": r - ref}), flush=True)
 
 
-def run_warmstart_suite(args):
+def run_warmstart_suite(args, quiet=False):
     """Learned warm start (BASELINE config 5; with --scale 2 the c2-shape headline).
 
     Scenario: a deployed model exists for a base matrix (c1 or c2 shape); 50,000 new users
@@ -260,7 +263,12 @@ def run_warmstart_suite(args):
     big = args.scale >= 2.0
     base_spec = synth.C2 if big else synth.C1
     new_users = 50_000
-    out = lambda d: print(json.dumps({"suite": "warmstart", "shape": "c2" if big else "c1", **d}), flush=True)
+    results = []
+
+    def out(d):
+        results.append(d)
+        if not quiet:
+            print(json.dumps({"suite": "warmstart", "shape": "c2" if big else "c1", **d}), flush=True)
 
     def solve(tr, m, n, seed, precision="fp16", iters=20, init=None, te=None, alpha=0.08, tail_epochs=0,
               tail_start=0, beta=0.3):
@@ -370,11 +378,31 @@ def run_warmstart_suite(args):
             w_ms, w_ep = time_to_target(wrm, wms)
             total = None if w_ms is None else w_ms + prep_ms
             out({"arm": f"warm {precision} alpha={alpha} beta={beta} new-user epochs={tail}" +
-                        ("" if use_mlp else " (no MLP: random new users)"),
+                        ("" if use_mlp else " (no MLP: random new users)"), "mlp": use_mlp,
                  "prep_ms": prep_ms, "new_user_test_rmse_at_init": init_new,
                  "epoch_rmse": [round(x, 5) for x in wrm], "epoch_ms": [round(x, 3) for x in wms],
                  "time_to_target_ms": total, "epochs_to_target": w_ep,
                  "speedup_vs_cold": (cold_ms / total) if (cold_ms and total) else None})
+    return {"target_rmse": target, "fp64_oracle_rmse": oracle_rmse, "cold_fp16_ms": cold_ms,
+            "cold_epochs": cold_ep, "arms": [r for r in results if "arm" in r and r["arm"] != "cold fp16"]}
+
+
+def warm_summary(args):
+    """Time-to-target line for bench.py's default run: c2 shape, cold fp16 against the MLP
+    warm start with bf16 stochastic rounding (one schedule) and its no-MLP ablation."""
+    a = argparse.Namespace(**vars(args))
+    a.scale, a.mlp_epochs, a.e2e_epochs = 2.0, 10, 20
+    a.warm_configs = "bf16sr:0.04:0.3:4"
+    r = run_warmstart_suite(a, quiet=True)
+    warm = next(x for x in r["arms"] if x.get("mlp"))
+    abl = next((x for x in r["arms"] if not x.get("mlp")), None)
+    return {"shape": "c2 base 480189x17770 (99.07M ratings) + 50000 new users (+5% ratings), k=128",
+            "target_rmse": r["target_rmse"], "target": "FP64 oracle (host threads) test RMSE + 0.002",
+            "cold_fp16_ms": r["cold_fp16_ms"], "cold_fp16_epochs": r["cold_epochs"],
+            "warm_bf16sr_ms": warm["time_to_target_ms"], "warm_bf16sr_epochs": warm["epochs_to_target"],
+            "warm_prep_ms": warm["prep_ms"], "warm_schedule": warm["arm"],
+            "speedup": warm["speedup_vs_cold"],
+            "no_mlp_ablation_ms": abl["time_to_target_ms"] if abl else None}
 
 
 def run_batched_suite(args):
@@ -541,6 +569,7 @@ def main():
     ap.add_argument("--e2e-epochs", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="skip the time-to-target measurement")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
     ap.add_argument("--mlp-epochs", type=int, default=30)
@@ -669,6 +698,14 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_port_baseline(train, m, n, seconds_budget=args.ref_seconds)
 
+    ttt = None
+    if rank == 0 and world == 1 and not args.no_warm:
+        del train, test
+        try:
+            ttt = warm_summary(args)
+        except Exception as e:  # reported, never fatal to the throughput line
+            ttt = {"error": repr(e)[:300]}
+
     if rank == 0:
         line = {"metric": "sgd_updates_per_sec", "value": updates_per_sec, "unit": "updates/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -681,7 +718,8 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(),
                              "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
-                "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu}
+                "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu,
+                "time_to_target": ttt}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -4,21 +4,29 @@
 //
 // Used by the warm-start MLP (forward: activations x W^T; backward: dX = dY W and
 // dW = dY^T X, given as TN products on transposed copies).  One CTA of 128 threads computes a
-// 128 x BN tile:
-//   - operand tiles of 64 K-elements are copied with cp.async into shared memory in the
-//     tcgen05 no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix; the
-//     K-adjacent core matrix at +128 bytes, the next 8 rows at +1024 bytes), two stages;
-//   - one elected thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=BN, K=16) four
-//     times per stage, accumulating in tensor memory (BN fp32 columns allocated with
-//     tcgen05.alloc), and tcgen05.commit arrives on an mbarrier per stage;
-//   - the epilogue reads the accumulator with tcgen05.ld (32 lanes x 32 columns per warp),
-//     adds the bias, applies the activation and stores bf16 or fp32.
+// 128 x BN tile (BN = 128 or 256):
+//   - thread 0 is the TMA producer: operand tiles of 64 K-elements (128-byte rows) arrive by
+//     cp.async.bulk.tensor.2d with the 128-byte swizzle into a 4-stage ring of shared memory,
+//     each stage guarded by a `full` mbarrier (armed with the expected byte count) and an
+//     `empty` mbarrier;
+//   - thread 32 issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=BN, K=16) four times per
+//     stage, accumulating in tensor memory (BN fp32 columns from tcgen05.alloc), and
+//     tcgen05.commit releases the stage to the producer through `empty`;
+//   - after the last stage a commit to `done` releases the epilogue, in which all four warps
+//     read the accumulator with tcgen05.ld (32 lanes x 32 columns per warp), add the bias,
+//     apply the activation and write 16-byte vectors of bf16 or fp32;
+//   - when the output has too few tiles to fill the GPU and K is long (the weight gradients),
+//     K is split over grid.z and the partial tiles are added into a zeroed fp32 output with
+//     vector atomics.
 // Every mbarrier wait is bounded; on timeout the kernel records CUMF_ERR_TIMEOUT, stops
 // issuing work, waits (bounded) for what it issued and releases its tensor memory.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "cumf_sgd.h"
 #include "internal.h"
@@ -36,26 +44,11 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte offset >> 4
-// (16-29), stride byte offset >> 4 (32-45), descriptor version 1 (46-47), base offset 0,
-// relative LBO mode, no swizzle (61-63 = 0).
-__device__ __forceinline__ uint64_t mat_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
-    return d;
-}
-
 // Instruction descriptor for kind::f16: D fp32 (bits 4-5 = 1), A and B bf16 (7-9, 10-12 = 1),
 // both K-major (15, 16 = 0), N >> 3 at 17-22, M >> 4 at 24-28.
 template <int BN>
 __device__ __forceinline__ uint32_t instr_desc() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
-}
-
-__device__ __forceinline__ void cp16(uint32_t dst, const void *src, uint32_t src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
@@ -77,48 +70,139 @@ __device__ __forceinline__ float gelu(float x) {
     return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
 }
 
-// Copies a rows x 64 bf16 tile (rows from r0, K from k0) into the core-matrix layout.
-// Out-of-range rows are zero-filled.
-template <int ROWS>
-__device__ __forceinline__ void load_tile(uint32_t sdst, const __nv_bfloat16 *G, int nrows, int K, int r0, int k0) {
-    constexpr int CHUNKS = ROWS * (kTcBK / 8);
-#pragma unroll 4
-    for (int c = threadIdx.x; c < CHUNKS; c += kTcThreads) {
-        const int row = c >> 3, kc = c & 7;
-        const int gr = r0 + row;
-        const bool ok = gr < nrows;
-        const __nv_bfloat16 *src = G + (size_t)(ok ? gr : 0) * K + k0 + kc * 8;
-        const uint32_t dst = sdst + (uint32_t)(((row >> 3) * 8 + kc) * 128 + (row & 7) * 16);
-        cp16(dst, src, ok ? 16u : 0u);
+constexpr int kStages = 4;
+
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;              // leading byte offset: unused for swizzled K-major
+    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset: one 8-row atom
+    d |= (uint64_t)1 << 46;              // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;              // 128-byte swizzle
+    return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+// Writes 32 consecutive accumulator columns of one output row (col0 .. col0+31, clipped at N):
+// fp32 partial sums by atomics (split K), or bias + activation into fp32 / bf16, with the
+// pre-activation copy when asked.  Whole in-range chunks on 16-byte aligned rows use vectors.
+__device__ __forceinline__ void store_chunk(const uint32_t (&r)[32], int row, int col0, int N,
+                                            const float *__restrict__ bias, int act, void *out, int out_f32,
+                                            int ldo, float *pre_out, bool partial) {
+    float v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    const bool whole = col0 + 32 <= N;
+    const size_t off = (size_t)row * ldo + col0;
+    if (partial) {
+        float *o = reinterpret_cast<float *>(out) + off;
+        if (whole && (ldo & 3) == 0) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) atomicAdd(reinterpret_cast<float4 *>(o + j), make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]));
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (col0 + j < N) atomicAdd(o + j, v[j]);
+        }
+        return;
+    }
+    if (bias) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (col0 + j < N) v[j] += bias[col0 + j];
+    }
+    if (pre_out) {
+        float *o = pre_out + off;
+        if (whole && (ldo & 3) == 0) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (col0 + j < N) o[j] = v[j];
+        }
+    }
+    if (act == 1) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = gelu(v[j]);
+    }
+    if (out_f32) {
+        float *o = reinterpret_cast<float *>(out) + off;
+        if (whole && (ldo & 3) == 0) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (col0 + j < N) o[j] = v[j];
+        }
+    } else {
+        __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + off;
+        if (whole && (ldo & 7) == 0) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 8) {
+                uint4 w;
+                __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) h[q] = __floats2bfloat162_rn(v[j + 2 * q], v[j + 2 * q + 1]);
+                *reinterpret_cast<uint4 *>(o + j) = w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (col0 + j < N) o[j] = __float2bfloat16_rn(v[j]);
+        }
     }
 }
 
 template <int BN>
-struct TcSmem {
-    static constexpr int A_BYTES = kTcBM * kTcBK * 2;
-    static constexpr int B_BYTES = BN * kTcBK * 2;
+struct TmaSmem {
+    static constexpr int A_BYTES = kTcBM * 128;  // 128 rows x 64 bf16
+    static constexpr int B_BYTES = BN * 128;
     static constexpr int STAGE = A_BYTES + B_BYTES;
-    static constexpr int TOTAL = 2 * STAGE + 64;  // + mbarriers and the TMEM address
+    static constexpr int TOTAL = 1024 + kStages * STAGE + 256;  // alignment slack + barriers
 };
 
 template <int BN>
 __global__ void __launch_bounds__(kTcThreads, 1)
-tc_gemm_kernel(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B, int M, int N, int K,
-               const float *__restrict__ bias, int act, void *out, int out_f32, int ldo, float *pre_out,
-               int *status) {
-    using S = TcSmem<BN>;
-    extern __shared__ __align__(1024) unsigned char smem[];
-    const uint32_t sbase = smem_u32(smem);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * S::STAGE);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 2 * S::STAGE + 32);
-    const uint32_t mbar0 = smem_u32(&mbar[0]), mbar1 = smem_u32(&mbar[1]);
+tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
+                   int N, int K, const float *__restrict__ bias, int act, void *out, int out_f32, int ldo,
+                   float *pre_out, int *status, int splits) {
+    using S = TmaSmem<BN>;
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;  // swizzle atoms need 1024-byte alignment
+    unsigned char *bar_area = smem_raw + (base - raw) + kStages * S::STAGE;
+    uint64_t *full = reinterpret_cast<uint64_t *>(bar_area);
+    uint64_t *empty = full + kStages;
+    uint64_t *done = empty + kStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+    int *issued_slot = abort_flag + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * BN;
+    const int KT_all = (K + kTcBK - 1) / kTcBK;
+    const int kt0 = (int)((long long)KT_all * blockIdx.z / splits);
+    const int kt1 = (int)((long long)KT_all * (blockIdx.z + 1) / splits);
+    const int KT = kt1 - kt0;
 
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar1));
+        for (int i = 0; i < kStages; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(done)));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        *abort_flag = 0;
+        *issued_slot = 0;
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
@@ -130,63 +214,63 @@ tc_gemm_kernel(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restr
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    const int KT = K / kTcBK;
-    bool alive = true;
-    // stage 0 <- k-tile 0
-    load_tile<kTcBM>(sbase, A, M, K, m0, 0);
-    load_tile<BN>(sbase + S::A_BYTES, B, N, K, n0, 0);
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    for (int kt = 0; kt < KT && alive; ++kt) {
-        const int st = kt & 1;
-        if (kt + 1 < KT) {
-            if (kt >= 1) {  // stage st^1 was read by the MMAs of k-tile kt-1
-                const int timed_out = !mbar_wait(st ? mbar0 : mbar1, ((kt - 1) >> 1) & 1);
-                if (__syncthreads_or(timed_out)) {  // every thread takes the same branch
-                    alive = false;
-                    break;
-                }
+    if (threadIdx.x == 0 && KT > 0) {  // TMA producer
+        for (int i = 0; i < KT; ++i) {
+            const int st = i % kStages;
+            if (i >= kStages && !mbar_wait(smem_u32(&empty[st]), ((i / kStages) - 1) & 1)) {
+                atomicExch(abort_flag, 1);
+                break;
             }
-            const uint32_t nb = sbase + (st ^ 1) * S::STAGE;
-            load_tile<kTcBM>(nb, A, M, K, m0, (kt + 1) * kTcBK);
-            load_tile<BN>(nb + S::A_BYTES, B, N, K, n0, (kt + 1) * kTcBK);
-            asm volatile("cp.async.commit_group;\n" ::: "memory");
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            const uint32_t fb = smem_u32(&full[st]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(S::STAGE)
+                         : "memory");
+            const uint32_t a_dst = base + st * S::STAGE;
+            tma_load_2d(a_dst, &map_a, (kt0 + i) * kTcBK, m0, fb);
+            tma_load_2d(a_dst + S::A_BYTES, &map_b, (kt0 + i) * kTcBK, n0, fb);
+            *issued_slot = i + 1;
         }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async writes -> tensor core reads
-        __syncthreads();
-        if (threadIdx.x == 0) {
+    } else if (threadIdx.x == 32 && KT > 0) {  // MMA issuer
+        for (int i = 0; i < KT; ++i) {
+            const int st = i % kStages;
+            if (!mbar_wait(smem_u32(&full[st]), (i / kStages) & 1)) {
+                atomicExch(abort_flag, 1);
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t a0 = sbase + st * S::STAGE, b0 = a0 + S::A_BYTES;
+            const uint32_t a0 = base + st * S::STAGE, b0 = a0 + S::A_BYTES;
 #pragma unroll
             for (int s = 0; s < kTcBK / 16; ++s) {
-                const uint64_t ad = mat_desc(a0 + s * 256, 128, 1024);
-                const uint64_t bd = mat_desc(b0 + s * 256, 128, 1024);
-                const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
+                const uint32_t acc = (i > 0 || s > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(instr_desc<BN>()), "r"(acc));
+                    "l"(sw128_desc(a0 + s * 32)), "l"(sw128_desc(b0 + s * 32)), "r"(instr_desc<BN>()), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             st ? mbar1 : mbar0)
+                             smem_u32(&empty[st]))
                          : "memory");
         }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         smem_u32(done))
+                     : "memory");
     }
-    // The last commit covers every MMA issued before it.
-    bool done = false;
-    if (alive && KT > 0) {
-        const int last = KT - 1;
-        done = __syncthreads_and(mbar_wait((last & 1) ? mbar1 : mbar0, (last >> 1) & 1));
-    }
-    if (!done || !alive) {
-        if (threadIdx.x == 0 && status) atomicExch(status, (int)CUMF_ERR_TIMEOUT);
-        asm volatile("cp.async.wait_all;\n" ::: "memory");
-        // Bounded drain of anything still in flight on either stage before the memory is freed.
-        mbar_wait(mbar0, 0);
-        mbar_wait(mbar1, 0);
-    } else {
+    // Everyone waits for the accumulator (bounded), then agrees on whether it is valid.
+    int ok = 1;
+    if (KT > 0) ok = mbar_wait(smem_u32(done), 0) ? 1 : 0;
+    __syncwarp();
+    ok = __syncthreads_and(ok && (*abort_flag == 0));
+    if (!ok) {
+        if (threadIdx.x == 0) {
+            if (status) atomicExch(status, (int)CUMF_ERR_TIMEOUT);
+            // Bounded drain: the last copy issued into each stage, then every MMA.
+            const int issued = *issued_slot;
+            for (int st = 0; st < kStages && st < issued; ++st) {
+                const int last = st + ((issued - 1 - st) / kStages) * kStages;
+                mbar_wait(smem_u32(&full[st]), (last / kStages) & 1);
+            }
+            mbar_wait(smem_u32(done), 0);
+        }
+    } else if (KT > 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const int row = m0 + warp * 32 + lane;
         for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -203,21 +287,8 @@ tc_gemm_kernel(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restr
                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (row < M) {
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int col = n0 + c0 + j;
-                    if (col < N) {
-                        float v = __uint_as_float(r[j]) + (bias ? bias[col] : 0.f);
-                        if (pre_out) pre_out[(size_t)row * ldo + col] = v;
-                        if (act == 1) v = gelu(v);
-                        if (out_f32)
-                            reinterpret_cast<float *>(out)[(size_t)row * ldo + col] = v;
-                        else
-                            reinterpret_cast<__nv_bfloat16 *>(out)[(size_t)row * ldo + col] = __float2bfloat16_rn(v);
-                    }
-                }
-            }
+            const int col0 = n0 + c0;
+            if (row < M && col0 < N) store_chunk(r, row, col0, N, bias, act, out, out_f32, ldo, pre_out, splits > 1);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -227,27 +298,72 @@ tc_gemm_kernel(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restr
     }
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// rows x K bf16 row-major operand, tiles of box_rows x 64 with 128-byte swizzle.
+bool make_map(CUtensorMap *map, const void *ptr, int rows, int K, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, const float *bias, int act,
                            void *out, int out_f32, int ldo, float *pre_out, int *status, cudaStream_t s) {
-    if (M <= 0 || N <= 0 || K <= 0 || (K % kTcBK) != 0) return cudaErrorInvalidValue;
+    if (M <= 0 || N <= 0 || K <= 0 || (K % 8) != 0) return cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15)) return cudaErrorInvalidValue;
     const bool wide = N > 128;
-    const dim3 grid((M + kTcBM - 1) / kTcBM, (N + (wide ? 256 : 128) - 1) / (wide ? 256 : 128));
+    const int BN = wide ? 256 : 128;
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, BN)) return cudaErrorInvalidValue;
+    const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + BN - 1) / BN;
+    const int kt = (K + kTcBK - 1) / kTcBK;
+    // Split K when the output has too few tiles to fill the GPU and K is long (weight gradients).
+    int splits = 1;
+    const bool plain = out_f32 && !bias && act == 0 && !pre_out;
+    if (plain && tiles_m * tiles_n < 152 && kt >= 16) {
+        splits = std::min(kt / 8, std::max(1, 2 * 152 / (tiles_m * tiles_n)));
+        cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
+        if (e != cudaSuccess) return e;
+    }
+    const dim3 grid(tiles_m, tiles_n, splits);
     if (wide) {
-        const int sm = TcSmem<256>::TOTAL;
-        cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        const int sm = TmaSmem<256>::TOTAL;
+        cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         if (e != cudaSuccess) return e;
-        tc_gemm_kernel<256><<<grid, kTcThreads, sm, s>>>(reinterpret_cast<const __nv_bfloat16 *>(A),
-                                                         reinterpret_cast<const __nv_bfloat16 *>(B), M, N, K, bias,
-                                                         act, out, out_f32, ldo, pre_out, status);
+        tc_gemm_tma_kernel<256><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
+                                                             status, splits);
     } else {
-        const int sm = TcSmem<128>::TOTAL;
-        cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        const int sm = TmaSmem<128>::TOTAL;
+        cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         if (e != cudaSuccess) return e;
-        tc_gemm_kernel<128><<<grid, kTcThreads, sm, s>>>(reinterpret_cast<const __nv_bfloat16 *>(A),
-                                                         reinterpret_cast<const __nv_bfloat16 *>(B), M, N, K, bias,
-                                                         act, out, out_f32, ldo, pre_out, status);
+        tc_gemm_tma_kernel<128><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
+                                                             status, splits);
     }
     return cudaGetLastError();
 }
@@ -258,8 +374,8 @@ using namespace cumf;
 
 extern "C" int cumf_tc_gemm(const void *d_A, const void *d_B, int M, int N, int K, const float *d_bias, int act,
                             void *d_out, int out_f32, int ldo, float *d_pre, int *d_status, void *stream) {
-    if (!d_A || !d_B || !d_out || M <= 0 || N <= 0 || K <= 0 || (K % 64) != 0 || ldo < N)
-        return fail(CUMF_ERR_ARG, "tc_gemm: bad arguments (K must be a multiple of 64, ldo >= N)");
+    if (!d_A || !d_B || !d_out || M <= 0 || N <= 0 || K <= 0 || (K % 8) != 0 || ldo < N)
+        return fail(CUMF_ERR_ARG, "tc_gemm: bad arguments (K must be a multiple of 8, ldo >= N)");
     if (act != 0 && act != 1) return fail(CUMF_ERR_ARG, "tc_gemm: act must be 0 (identity) or 1 (gelu)");
     CUMF_CUDA(launch_tc_gemm(d_A, d_B, M, N, K, d_bias, act, d_out, out_f32, ldo, d_pre, d_status,
                              (cudaStream_t)stream));

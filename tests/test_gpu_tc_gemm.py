@@ -20,7 +20,7 @@ def ref(A, B, bias, act):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 512, 192), (300, 144, 128), (1000, 128, 512),
-                                   (77, 256, 64), (130, 520, 64)])
+                                   (77, 256, 64), (130, 520, 64), (200, 136, 136), (129, 264, 40)])
 @pytest.mark.parametrize("act", [0, 1])
 def test_tc_gemm_matches_torch_fp32(lib, cuda, M, N, K, act):
     import torch
@@ -55,3 +55,24 @@ def test_tc_gemm_rejects_bad_k(lib, cuda):
     out = torch.zeros(128, 128, dtype=torch.float32, device=cuda)
     assert lib.cumf_tc_gemm(A.data_ptr(), A.data_ptr(), 128, 128, 100, None, 0, out.data_ptr(), 1, 128, None,
                             None, None) != 0
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 512, 16384), (131, 200, 4104), (512, 192, 65536)])
+def test_tc_gemm_split_k_matches_torch_fp32(lib, cuda, M, N, K):
+    """Plain fp32 products with few output tiles and long K (the weight-gradient shapes) are
+    split over K and summed with atomics into the zeroed output."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(M + N + K)
+    A = (torch.randn(M, K, generator=g) * 0.5).to(torch.bfloat16).to(cuda)
+    B = (torch.randn(N, K, generator=g) * 0.5).to(torch.bfloat16).to(cuda)
+    out = torch.full((M, N), float("nan"), dtype=torch.float32, device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    for _ in range(2):  # the output is overwritten, not accumulated across calls
+        rc = lib.cumf_tc_gemm(A.data_ptr(), B.data_ptr(), M, N, K, None, 0, out.data_ptr(), 1, N, None,
+                              status.data_ptr(), None)
+        assert rc == 0, lib.cumf_last_error()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    exp = A.float() @ B.float().T
+    scale = exp.abs().max().item()
+    assert (out - exp).abs().max().item() <= 1e-4 * scale + 1e-6
