@@ -566,6 +566,9 @@ def main():
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--workers", type=int, default=0)
     ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--prefetch", type=int, default=-1, help="L2 prefetch distance in records (-1: default)")
+    ap.add_argument("--l2-hints", type=int, default=-1, help="L2 eviction hints 0/1 (-1: default)")
+    ap.add_argument("--ring", type=int, default=-1, help="shared-memory row ring 0/1 (-1: default)")
     ap.add_argument("--e2e-epochs", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -640,7 +643,8 @@ def main():
 
     def epoch(e):
         cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m, Q.data_ptr(), n, K, prec, workers, args.lanes,
-                      lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp)
+                      lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp,
+                      prefetch=args.prefetch, l2_hints=args.l2_hints, ring=args.ring)
 
     for e in range(args.warmup):
         epoch(e)
