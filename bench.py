@@ -549,6 +549,100 @@ def run_gemm_suite(args):
                           "peak_tflops": peak, "frac": tf / peak, "max_abs_err_vs_fp32": err}), flush=True)
 
 
+def ratings_text_gpu(train, header: bytes):
+    """The records as rating text ("u v r" lines, integer ratings), built on the GPU: digits in
+    fixed-width rows, then the padding bytes dropped with one masked select."""
+    import torch
+    dev = torch.device("cuda", 0)
+    u = torch.from_numpy(train["u"].astype(np.int64)).to(dev)
+    v = torch.from_numpy(train["v"].astype(np.int64)).to(dev)
+    r = torch.from_numpy(np.rint(train["r"]).astype(np.int64)).to(dev)
+
+    def digits(x, width):
+        pw = 10 ** torch.arange(width - 1, -1, -1, device=dev)
+        d = (x[:, None] // pw) % 10
+        nd = torch.clamp((x[:, None] >= pw).sum(1), min=1)
+        keep = torch.arange(width, device=dev)[None, :] >= (width - nd)[:, None]
+        return (d + 48).to(torch.uint8), keep
+
+    du, ku = digits(u, 10)
+    dv, kv = digits(v, 10)
+    dr, kr = digits(r, 2)
+    n = len(train)
+    sp = torch.full((n, 1), 32, dtype=torch.uint8, device=dev)
+    nl = torch.full((n, 1), 10, dtype=torch.uint8, device=dev)
+    one = torch.ones((n, 1), dtype=torch.bool, device=dev)
+    rows = torch.cat([du, sp, dv, sp, dr, nl], 1)
+    keep = torch.cat([ku, one, kv, one, kr, one], 1)
+    body = rows[keep]
+    head = torch.frombuffer(bytearray(header), dtype=torch.uint8).to(dev)
+    return torch.cat([head, body, torch.zeros(16, dtype=torch.uint8, device=dev)])
+
+
+def run_text_suite(args):
+    """Rating text -> records (data/netflix/transform.cpp) for the c2 ratings as text: device
+    parse (text resident in HBM) and end to end from pinned host text to pinned host records,
+    against the oracle's strtol/strtof parse of a bounded sample on one host core."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+    from oracle import oracle
+    build.build()
+    spec = synth.C2 if args.scale >= 1.0 else synth.scaled(synth.C2, args.scale)
+    train, _ = synth.generate(spec, seed=0, device="cuda")
+    header = b"%%%%MatrixMarket matrix coordinate real general\n%% c2 synthetic\n%d %d %d\n" % (
+        spec.m, spec.n, len(train))
+    d_text = ratings_text_gpu(train, header)
+    length = d_text.numel() - 16
+    n = len(train)
+    start = len(header)
+    d_out = torch.empty(n * 12, dtype=torch.uint8, device=d_text.device)
+    h_text = d_text.cpu().pin_memory()
+    h_out = torch.empty(n * 12, dtype=torch.uint8).pin_memory()
+    stream = torch.cuda.current_stream()
+
+    def device_parse():
+        assert cm.dev_parse_text(d_text.data_ptr(), length, start, d_out.data_ptr(), n) == n
+
+    def end_to_end():
+        d_text[:length].copy_(h_text[:length], non_blocking=True)
+        device_parse()
+        h_out.copy_(d_out, non_blocking=True)
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        end_to_end()
+    got = h_out.numpy().view(synth.NODE_DTYPE)
+    ok = bool(np.array_equal(got["u"], train["u"]) and np.array_equal(got["v"], train["v"]) and
+              np.array_equal(got["r"], np.rint(train["r"]).astype(np.float32)))
+    res = {}
+    for name, fn in (("device", device_parse), ("e2e", end_to_end)):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "wall_ms": wall * 1e3}
+    # Oracle (strtol/strtof, one core) on a bounded prefix of the same text.
+    sample_lines = min(n, 4_000_000)
+    cut = int(np.searchsorted(np.cumsum(h_text[start:length].numpy() == 10), sample_lines)) + start + 1
+    sample = h_text[:cut].numpy().tobytes()
+    t0 = time.perf_counter()
+    recs = oracle.parse_text(sample)
+    cpu_s = time.perf_counter() - t0
+    print(json.dumps({"suite": "text", "records": n, "text_bytes": length, "parse_matches_records": ok,
+                      "device_ms": res["device"]["ms"], "device_GBps": length / res["device"]["ms"] / 1e6,
+                      "device_records_per_s": n / res["device"]["ms"] * 1e3,
+                      "e2e_ms": res["e2e"]["ms"], "e2e_records_per_s": n / res["e2e"]["ms"] * 1e3,
+                      "e2e_h2d_bytes": length, "e2e_d2h_bytes": n * 12,
+                      "cpu_oracle": {"records": len(recs), "seconds": cpu_s, "records_per_s": len(recs) / cpu_s,
+                                     "cores": 1, "kind": "port (strtol/strtof)"}}), flush=True)
+
+
 def _has_cuda():
     try:
         import torch
@@ -579,7 +673,7 @@ def main():
     ap.add_argument("--warm-configs",
                     default="bf16sr:0.04:0.3:4,bf16sr:0.02:0.05:8,bf16sr:0.04:0.3:2,fp16:0.04:0.3:4,bf16sr:0.02:0.3:0",
                     help="warm-start refinements as storage:alpha:beta:new_user_epochs, comma separated")
-    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm"],
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm", "text"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
     if args.suite == "precision":
@@ -593,6 +687,9 @@ def main():
         return
     if args.suite == "gemm":
         run_gemm_suite(args)
+        return
+    if args.suite == "text":
+        run_text_suite(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -168,6 +168,39 @@ def read_problem(path: str, pinned: bool = True) -> MFProblem:
     return MFProblem(c)
 
 
+def convert_text(in_path: str, out_path: Optional[str] = None, header_lines: int = 3) -> int:
+    """`./transform file_name` (data/netflix/transform.cpp:9-47) parsed on the GPU; returns
+    the number of 12-byte records written (to in_path + ".bin" by default)."""
+    n = C.c_int64(0)
+    _lib.check(_lib.load().cumf_convert_text(in_path.encode(), out_path.encode() if out_path else None,
+                                             header_lines, C.byref(n)))
+    return n.value
+
+
+def read_text_problem(path: str, header_lines: int = 3, pinned: bool = True) -> MFProblem:
+    """Rating text parsed on the GPU into a problem (what read_problem returns for the
+    converted file)."""
+    c = _lib.Problem()
+    _lib.check(_lib.load().cumf_read_text_problem(path.encode(), header_lines, int(pinned), C.byref(c)))
+    return MFProblem(c)
+
+
+def text_data_start(text: bytes, header_lines: int = 3) -> int:
+    """Offset of the first data byte after the header lines (transform.cpp:31-33)."""
+    out = C.c_int64(0)
+    _lib.check(_lib.load().cumf_text_data_start(text, len(text), header_lines, C.byref(out)))
+    return out.value
+
+
+def dev_parse_text(d_text: int, length: int, start: int, d_out: int = 0, cap: int = 0, stream: int = 0) -> int:
+    """Device text bytes [start, length) -> records at d_out; returns the record count
+    (d_out = 0: count only)."""
+    n = C.c_int64(0)
+    _lib.check(_lib.load().cumf_dev_parse_text(d_text, length, start, d_out or None, cap, C.byref(n),
+                                               stream or None))
+    return n.value
+
+
 class MFModel:
     """mf_model as written to the model file: fp32 P (m x k), Q (n x k) and b."""
 

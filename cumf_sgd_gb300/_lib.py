@@ -94,6 +94,11 @@ _SIGS = {
     "cumf_parse_args": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Args)]),
     "cumf_read_problem": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Problem)]),
     "cumf_write_problem": (C.c_int, [C.c_char_p, C.POINTER(Problem)]),
+    "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
+    "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),
+    "cumf_text_data_start": (C.c_int, [C.c_char_p, C.c_int64, C.c_int, C.POINTER(C.c_int64)]),
+    "cumf_dev_parse_text": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
+                                      C.POINTER(C.c_int64), C.c_void_p]),
     "cumf_alloc_problem": (C.c_int, [C.c_int64, C.c_int, C.POINTER(Problem)]),
     "cumf_free_problem": (C.c_int, [C.POINTER(Problem)]),
     "cumf_save_model": (C.c_int, [C.POINTER(Model), C.c_char_p]),

@@ -4,6 +4,7 @@ Outputs (all git-ignored, rebuilt on every machine):
   cumf_sgd_gb300/lib/libcumf_sgd.so   the C-ABI library (CUDA kernels for sm_103a + host code)
   cumf_sgd_gb300/bin/cumf_sgd         drop-in for singleGPU/cumf_sgd (main.cpp)
   cumf_sgd_gb300/bin/cumf_predict     RMSE evaluator (mf-predict -e 0)
+  cumf_sgd_gb300/bin/cumf_transform   rating text -> binary records (data/netflix/transform)
 Translation units compile in parallel; nothing here needs cmake.
 """
 from __future__ import annotations
@@ -34,8 +35,9 @@ LIB_SOURCES = [
     "tc_gemm.cu",
     "mlp.cu",
     "batch.cu",
+    "text_parse.cu",
 ]
-TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp"}
+TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp", "cumf_transform": "transform_main.cpp"}
 
 
 def nvcc() -> str:

@@ -188,6 +188,29 @@ int cumf_load_model(const char *path, cumf_model *out);
 int cumf_alloc_model(int32_t m, int32_t n, int32_t k, cumf_model *out);
 int cumf_free_model(cumf_model *model);
 
+/* ---- rating text (data/netflix/transform.cpp) --------------------------------------- */
+
+/* `./transform file_name` (data/netflix/transform.cpp:9-47) on the GPU: skips `header_lines`
+ * lines the way fscanf(f, "%[^\n]\n") does (the reference skips 3, transform.cpp:31-33),
+ * parses whitespace-separated "u v r" triples as fscanf("%d %d %f") does (transform.cpp:36)
+ * and writes the 12-byte records to out_path (NULL: in_path + ".bin", transform.cpp:26).
+ * Ratings are rounded to float exactly as strtof rounds.  Where fscanf would stop silently
+ * or write a record with stale fields (a malformed token, a trailing partial triple), this
+ * returns CUMF_ERR_FORMAT naming the byte offset; ids outside int32, hexadecimal floats and
+ * ratings needing more than 19 significant digits to round are also rejected.
+ * *n_records (may be NULL) receives the record count. */
+int cumf_convert_text(const char *in_path, const char *out_path, int header_lines, int64_t *n_records);
+/* The same parse into a problem (read_problem's result for the converted file, sgd.cu:190):
+ * m = max u + 1, n = max v + 1; negative ids are rejected. */
+int cumf_read_text_problem(const char *path, int header_lines, int pinned, cumf_problem *out);
+/* Host helper: offset of the first data byte after `header_lines` header lines. */
+int cumf_text_data_start(const char *text, int64_t len, int header_lines, int64_t *start);
+/* Device-level parse of text bytes [start, len) of d_text (16-byte aligned device memory)
+ * into d_out.  *n_records receives the record count; with d_out == NULL only the count is
+ * computed.  A d_out with cap < count fails with CUMF_ERR_ARG. Synchronises the stream. */
+int cumf_dev_parse_text(const void *d_text, int64_t len, int64_t start, cumf_node *d_out, int64_t cap,
+                        int64_t *n_records, void *stream);
+
 /* ---- training --------------------------------------------------------------------- */
 /* sgd_train (singleGPU/sgd.cu:638-690): stats -> shuffle ids -> grid -> scale -> init ->
  * batch-Hogwild epochs -> fp32 export, unscale, un-permute.  `va` may be NULL; when given,

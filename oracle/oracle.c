@@ -5,6 +5,8 @@
  */
 #include "oracle.h"
 
+#include <ctype.h>
+#include <errno.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -611,4 +613,70 @@ void or_sgd_epochs_f64_threads(or_sgd64_args *a, int threads) {
     for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
     free(th);
     free(args);
+}
+
+
+/* ---- rating text (data/netflix/transform.cpp:31-42) ------------------------------------- */
+
+static int or_space(unsigned char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
+
+int64_t or_parse_text(const char *text, int64_t len, int header_lines, or_node *out, int64_t cap,
+                      int64_t *bad_offset) {
+    const unsigned char *p = (const unsigned char *)text;
+    int64_t i = 0, ntok = 0;
+    /* fscanf(file_in, "%[^\n]\n", line) x header_lines (transform.cpp:31-33): the scanset
+     * needs at least one character, so an empty line (or the end) stops this and later calls. */
+    for (int h = 0; h < header_lines; ++h) {
+        if (i >= len || p[i] == '\n') break;
+        while (i < len && p[i] != '\n') ++i;
+        while (i < len && or_space(p[i])) ++i;
+    }
+    char tok[1100];
+    or_node rec = {0, 0, 0.f};
+    while (1) {
+        while (i < len && or_space(p[i])) ++i;
+        if (i >= len) break;
+        const int64_t t0 = i;
+        while (i < len && !or_space(p[i])) ++i;
+        const int64_t tl = i - t0;
+        if (tl >= (int64_t)sizeof(tok)) {
+            *bad_offset = t0;
+            return -1;
+        }
+        memcpy(tok, p + t0, (size_t)tl);
+        tok[tl] = 0;
+        const int field = (int)(ntok % 3);
+        char *end = NULL;
+        errno = 0;
+        if (field < 2) {
+            /* %d: optional sign and decimal digits only */
+            const char *q = tok + ((tok[0] == '+' || tok[0] == '-') ? 1 : 0);
+            int ok = *q != 0;
+            for (const char *c = q; *c; ++c) ok &= isdigit((unsigned char)*c) != 0;
+            long long v = ok ? strtoll(tok, &end, 10) : 0;
+            if (!ok || errno == ERANGE || v < INT32_MIN || v > INT32_MAX) {
+                *bad_offset = t0;
+                return -1;
+            }
+            if (field == 0)
+                rec.u = (int32_t)v;
+            else
+                rec.v = (int32_t)v;
+        } else {
+            /* %f: decimal, inf/infinity or nan; no hexadecimal forms or nan(...) payloads */
+            const char *q = tok + ((tok[0] == '+' || tok[0] == '-') ? 1 : 0);
+            const int hex = q[0] == '0' && (q[1] == 'x' || q[1] == 'X');
+            const int paren = strchr(tok, '(') != NULL;
+            float f = hex || paren ? 0.f : strtof(tok, &end);
+            if (hex || paren || end != tok + tl) {
+                *bad_offset = t0;
+                return -1;
+            }
+            rec.r = f;
+            if (out && ntok / 3 < cap) out[ntok / 3] = rec;
+        }
+        ++ntok;
+    }
+    if (ntok % 3 != 0) return -2;
+    return ntok / 3;
 }

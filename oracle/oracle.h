@@ -150,6 +150,15 @@ void or_sgd_epochs_f64_threads(or_sgd64_args *a, int threads);
 double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t m, const double *Q,
                         int32_t n, int k, double b);
 
+/* data/netflix/transform.cpp:31-42 (the strict form the GPU converter implements): skips
+ * `header_lines` lines as fscanf(f, "%[^\n]\n") does, then reads whitespace-separated
+ * triples, u and v with strtol (the conversion behind %d) and r with strtof (behind %f).
+ * Returns the record count, or -1 with *bad_offset = byte offset of the first token that is
+ * not a complete decimal integer in int32 (u, v) or a complete decimal / inf / nan float (r),
+ * or -2 when the token count is not a multiple of 3.  out may be NULL (count only). */
+int64_t or_parse_text(const char *text, int64_t len, int header_lines, or_node *out, int64_t cap,
+                      int64_t *bad_offset);
+
 #ifdef __cplusplus
 }
 #endif

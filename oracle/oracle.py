@@ -121,6 +121,9 @@ def lib() -> C.CDLL:
         _lib.or_calc_rmse_f64.restype = C.c_double
         _lib.or_calc_rmse_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                           C.c_int, C.c_double]
+        _lib.or_parse_text.argtypes = [C.c_char_p, C.c_int64, C.c_int, C.c_void_p, C.c_int64,
+                                        C.POINTER(C.c_int64)]
+        _lib.or_parse_text.restype = C.c_int64
         _lib.or_hogwild_threads.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
                                             C.c_int32, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
                                             C.c_float, C.c_float, C.c_uint64, C.c_int]
@@ -303,3 +306,29 @@ def calc_rmse_f64(records: np.ndarray, P: np.ndarray, Q: np.ndarray, b: float) -
     P = np.ascontiguousarray(P, dtype=np.float64)
     Q = np.ascontiguousarray(Q, dtype=np.float64)
     return lib().or_calc_rmse_f64(_ptr(rec), len(rec), _ptr(P), P.shape[0], _ptr(Q), Q.shape[0], P.shape[1], b)
+
+
+def parse_text(text: bytes, header_lines: int = 3):
+    """Records of a rating text (transform.cpp:31-42, strict form), or ("bad", offset) /
+    ("partial", None) when the text is rejected."""
+    L = lib()
+    bad = C.c_int64(-1)
+    n = L.or_parse_text(text, len(text), header_lines, None, 0, C.byref(bad))
+    if n == -1:
+        return ("bad", bad.value)
+    if n == -2:
+        return ("partial", None)
+    out = np.zeros(n, dtype=NODE)
+    L.or_parse_text(text, len(text), header_lines, _ptr(out) if n else None, n, C.byref(bad))
+    return out
+
+
+def ref_transform(text: bytes, tmpdir: str) -> bytes:
+    """Output of the reference's own transform (oracle/_ref/transform) for a text."""
+    exe = os.path.join(REF_DIR, "transform")
+    path = os.path.join(tmpdir, "ratings")
+    with open(path, "wb") as f:
+        f.write(text)
+    subprocess.run([exe, path], check=True, capture_output=True)
+    with open(path + ".bin", "rb") as f:
+        return f.read()

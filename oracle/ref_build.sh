@@ -5,6 +5,7 @@
 #   mf-train, mf-predict   test/{mf.cpp,mf-train.cpp,mf-predict.cpp}, flags of test/Makefile
 #   ref_rmse               calc_rmse/mf_load_model/read_problem from test/mf.cpp
 #   ref_layout             singleGPU/sgd.cu host functions (id maps, shuffle, grid, scale)
+#   transform              data/netflix/transform.cpp (rating text -> 12-byte records)
 set -euo pipefail
 REF=${CUMF_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -24,4 +25,5 @@ nvcc -std=c++11 -O3 -w -gencode arch=compute_103a,code=sm_103a -I"$REF/singleGPU
 nvcc -std=c++11 -O3 -w -Wno-deprecated-declarations -I"$REF/singleGPU" \
      -c "$HERE/ref_layout_driver.cpp" -o "$OUT/ref_layout_driver.o"
 nvcc -o "$OUT/ref_layout" "$OUT/ref_layout_driver.o" "$OUT/sgd.o" -Xlinker --wrap=time -lcurand
+g++ -O2 -w -o "$OUT/transform" "$REF/data/netflix/transform.cpp"
 echo "built reference tools in $OUT"

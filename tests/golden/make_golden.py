@@ -6,7 +6,8 @@ reference tree is mounted):
                 collect_data / scale_problem / scale_model / shuffle_model
   ref_rmse    - test/mf.cpp read_problem + mf_load_model + calc_rmse (full precision)
   mf-predict  - test/mf-predict.cpp "-e 0" output line
-Usage: python tests/golden/make_golden.py   (rewrites layout_*.npz and rmse.npz)
+  transform   - data/netflix/transform.cpp (rating text -> 12-byte records)
+Usage: python tests/golden/make_golden.py   (rewrites layout_*.npz, rmse.npz and text.npz)
 """
 from __future__ import annotations
 
@@ -84,12 +85,66 @@ def rmse_fixtures(tmp: str) -> None:
                         **{f"{key}{i}": np.asarray(c[key]) for i, c in enumerate(cases) for key in c})
 
 
+def text_cases() -> dict:
+    """Rating texts the reference's transform accepts: MatrixMarket-style headers, integer and
+    decimal ratings in many spellings (exact float ties, the float range ends, subnormals,
+    inf/nan), ids with signs and leading zeros, and whitespace/header layouts."""
+    rng = np.random.default_rng(99)
+    head = b"%%MatrixMarket matrix coordinate real general\n% synthetic ratings\n1000 400 5000\n"
+    cases = {}
+    lines = [b"%d %d %d" % (rng.integers(0, 1000), rng.integers(0, 400), rng.integers(1, 6)) for _ in range(2000)]
+    cases["mm_int"] = head + b"\n".join(lines) + b"\n"
+    fmts = ["%.1f", "%.2f", "%.3f", "%.9g", "%.17g", "%.6e", "%g", "%.12f", "%.18e"]
+    vals = np.concatenate([rng.uniform(0, 5, 1500), rng.normal(0, 20, 700), 10.0 ** rng.uniform(-40, 38, 600),
+                           -(10.0 ** rng.uniform(-44, 30, 200))])
+    special = [b"0.1", b"0.2", b"0.3", b"1e-3", b"2.5E+1", b"+4", b"007", b"-0.0", b"4.", b".5", b"-.25",
+               b"1.000000000000000000", b"3.4028235677973366e38", b"3.4028234663852886e38",
+               b"3.4028235677973365e38", b"1.4e-45", b"7.006492321624086e-46", b"7.006492321624087e-46",
+               b"1.1754943508222875e-38", b"0.000000000000000000000000000000000000000001",
+               b"123456789012345678", b"16777217", b"16777219", b"9007199254740993", b"1.000000059604644775",
+               b"1.000000059604644776", b"0.1000000014901161193", b"33554431", b"1e39", b"1e-50",
+               b"inf", b"-inf", b"INF", b"Infinity", b"nan", b"-nan", b"NaN", b"5e0", b"5E-0", b"0e10",
+               b"00000000000000000000000000000000000000000000000001.5", b"1234567890123456789e-30"]
+    toks = [(fmts[i % len(fmts)] % x).encode() for i, x in enumerate(vals)] + special
+    ids = [b"+12", b"0003", b"-5", b"2147483647", b"-2147483648", b"0", b"+0", b"-0"]
+    lines = []
+    for i, t in enumerate(toks):
+        u = ids[i % len(ids)] if i % 7 == 0 else b"%d" % rng.integers(0, 100000)
+        lines.append(u + b" " + (b"%d" % rng.integers(0, 5000)) + b" " + t)
+    cases["decimals"] = head + b"\n".join(lines) + b"\n"
+    ws = [b" ", b"\t", b"  ", b" \t ", b"\r\n", b"\n\n", b"\v", b"\f"]
+    parts = []
+    for i in range(600):
+        rec = [b"%d" % rng.integers(0, 50), b"%d" % rng.integers(0, 50), b"%.2f" % rng.uniform(1, 5)]
+        parts.append(ws[rng.integers(0, len(ws))].join(rec) + ws[rng.integers(0, len(ws))])
+    cases["whitespace"] = b"h1 with spaces  \r\n\th2\nh3\n   " + b"".join(parts) + b"7 8 9.5"  # no final newline
+    cases["header_blank"] = b"h1\n\nh3\n1 2 3\n4 5 6\n"
+    cases["header_empty_first"] = b"\n1 2 3\n4 5 6.25\n"
+    cases["header_short"] = b"only one line"
+    cases["empty"] = b""
+    cases["one_record_spanning_lines"] = head + b"1\n2\n3.5\n"
+    return cases
+
+
+def text_fixtures(tmp: str) -> None:
+    out = {}
+    for name, text in text_cases().items():
+        out["text_" + name] = np.frombuffer(text, dtype=np.uint8)
+        out["bin_" + name] = np.frombuffer(oracle.ref_transform(text, tmp), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "text.npz"), **out)
+    print("wrote text.npz")
+
+
 def main() -> None:
     if not oracle.reference_available():
         oracle.build_reference()
     with tempfile.TemporaryDirectory() as tmp:
+        if len(sys.argv) > 1 and sys.argv[1] == "text":
+            text_fixtures(tmp)
+            return
         layout_fixtures(tmp)
         rmse_fixtures(tmp)
+        text_fixtures(tmp)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,132 @@
+"""GPU rating-text converter (data/netflix/transform.cpp) against the reference's own
+transform output (golden fixtures) and the oracle's strict parse on large random texts."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+pytestmark = pytest.mark.gpu
+
+
+def fixtures():
+    z = np.load(os.path.join(GOLDEN, "text.npz"))
+    return {k[5:]: (z[k].tobytes(), z["bin_" + k[5:]].tobytes()) for k in z.files if k.startswith("text_")}
+
+
+def test_convert_matches_reference_transform(lib, cuda, tmp_path):
+    import cumf_sgd_gb300 as cm
+    for name, (text, ref) in fixtures().items():
+        src = tmp_path / name
+        src.write_bytes(text)
+        n = cm.convert_text(str(src))
+        assert n * 12 == len(ref), name
+        assert (tmp_path / (name + ".bin")).read_bytes() == ref, name
+
+
+def test_transform_tool_writes_reference_records(lib, cuda, tmp_path):
+    text, ref = fixtures()["decimals"]
+    src = tmp_path / "netflix_train"
+    src.write_bytes(text)
+    exe = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_transform")
+    res = subprocess.run([exe, str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout
+    assert (tmp_path / "netflix_train.bin").read_bytes() == ref
+
+
+def random_text(n, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.integers(0, 2_000_000, n)
+    v = rng.integers(0, 20_000, n)
+    kind = rng.integers(0, 6, n)
+    r = np.where(kind == 0, rng.integers(1, 6, n).astype(np.float64),
+                 np.where(kind < 3, rng.uniform(0, 5, n), 10.0 ** rng.uniform(-44, 38, n)))
+    fmts = ["%d", "%.1f", "%.9g", "%.17g", "%.6e", "%.18e"]
+    seps = [" ", "\t", "  "]
+    ends = ["\n", "\r\n", " \n"]
+    out = ["%%MatrixMarket matrix coordinate real general\n%\n2000000 20000 %d\n" % n]
+    for i in range(n):
+        f = fmts[kind[i]]
+        rv = ("%d" % r[i]) if f == "%d" else (f % r[i])
+        out.append("%d%s%d%s%s%s" % (u[i], seps[i % 3], v[i], seps[(i + 1) % 3], rv, ends[i % 3]))
+    return "".join(out).encode()
+
+
+@pytest.mark.parametrize("n,seed", [(1, 1), (1000, 2), (300_000, 3)])
+def test_device_parse_matches_oracle(lib, cuda, orc, n, seed):
+    import torch
+    import cumf_sgd_gb300 as cm
+    text = random_text(n, seed)
+    exp = orc.parse_text(text)
+    assert len(exp) == n
+    d = torch.frombuffer(bytearray(text + b"\0" * 16), dtype=torch.uint8).to(cuda)
+    start = cm.text_data_start(text)
+    cnt = cm.dev_parse_text(d.data_ptr(), len(text), start)
+    assert cnt == n
+    out = torch.empty(n * 12, dtype=torch.uint8, device=cuda)
+    assert cm.dev_parse_text(d.data_ptr(), len(text), start, out.data_ptr(), n) == n
+    got = out.cpu().numpy().tobytes()
+    assert got == exp.tobytes()
+
+
+def test_read_text_problem_extent(lib, cuda, tmp_path):
+    import cumf_sgd_gb300 as cm
+    text = b"a\nb\nc\n3 7 1.5\n0 2 4\n12 0 2.25\n"
+    p = tmp_path / "t.txt"
+    p.write_bytes(text)
+    prob = cm.read_text_problem(str(p))
+    assert (prob.m, prob.n, prob.nnz) == (13, 8, 3)
+    assert list(prob.records["r"]) == [1.5, 4.0, 2.25]
+    p.write_bytes(b"a\nb\nc\n-3 7 1.5\n")
+    with pytest.raises(cm.CumfError):
+        cm.read_text_problem(str(p))
+
+
+@pytest.mark.parametrize("body,where", [
+    (b"1 2 3\n4 5 x\n", 10), (b"1 2.5 3\n", 2), (b"1 2 0x1p3\n", 4), (b"99999999999 2 3\n", 0),
+    (b"1 2 3.5.5\n", 4), (b"1 2 1e\n", 4), (b"1 2 --3\n", 4), (b"1 2 nan(1)\n", 4), (b"1 +-2 3\n", 2)])
+def test_malformed_tokens_fail_at_the_oracle_offset(lib, cuda, orc, tmp_path, body, where):
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import _lib
+    head = b"a\nb\nc\n"
+    assert orc.parse_text(head + body) == ("bad", len(head) + where)
+    p = tmp_path / "bad.txt"
+    p.write_bytes(head + body)
+    with pytest.raises(cm.CumfError) as e:
+        cm.convert_text(str(p))
+    assert e.value.code == _lib.CUMF_ERR_FORMAT
+    assert "byte %d:" % (len(head) + where) in str(e.value)
+
+
+def test_partial_triple_and_long_digits(lib, cuda, orc, tmp_path):
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import _lib
+    p = tmp_path / "t.txt"
+    p.write_bytes(b"a\nb\nc\n1 2 3 4\n")
+    with pytest.raises(cm.CumfError) as e:
+        cm.convert_text(str(p))
+    assert e.value.code == _lib.CUMF_ERR_FORMAT
+    # More than 19 significant digits: accepted when the dropped digits cannot change the
+    # rounding, rejected when they could (strtof would resolve it with all the digits).
+    p.write_bytes(b"a\nb\nc\n1 2 1.00000000000000000000001\n")
+    assert cm.convert_text(str(p)) == 1
+    ref = orc.parse_text(p.read_bytes())
+    assert (tmp_path / "t.txt.bin").read_bytes() == ref.tobytes()
+    p.write_bytes(b"a\nb\nc\n1 2 1.0000000596046447753906250000001\n")
+    with pytest.raises(cm.CumfError) as e:
+        cm.convert_text(str(p))
+    assert "19 significant digits" in str(e.value)
+
+
+def test_capacity_errors(lib, cuda):
+    import torch
+    import cumf_sgd_gb300 as cm
+    text = b"1 2 3\n4 5 6\n"
+    d = torch.frombuffer(bytearray(text + b"\0" * 16), dtype=torch.uint8).to(cuda)
+    out = torch.empty(12, dtype=torch.uint8, device=cuda)
+    with pytest.raises(cm.CumfError):
+        cm.dev_parse_text(d.data_ptr(), len(text), 0, out.data_ptr(), 1)
+    with pytest.raises(cm.CumfError):  # misaligned text
+        cm.dev_parse_text(d.data_ptr() + 1, len(text) - 1, 0)

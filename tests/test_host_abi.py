@@ -183,3 +183,23 @@ def test_cli_usage_errors(lib):
     exe2 = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_predict")
     res = subprocess.run([exe2, "-e", "1", "a", "b"], capture_output=True, text=True)
     assert res.returncode == 1
+
+
+def test_text_header_skip_follows_fscanf(lib):
+    """fscanf("%[^\\n]\\n") three times (transform.cpp:31-33): each call takes a non-empty line
+    and the whitespace after it; an empty line stops it."""
+    import cumf_sgd_gb300 as cm
+    assert cm.text_data_start(b"h1\n\nh3\n1 2 3\n4 5 6\n") == 13
+    assert cm.text_data_start(b"\n1 2 3\n") == 0
+    assert cm.text_data_start(b"only one line") == 13
+    assert cm.text_data_start(b"") == 0
+    assert cm.text_data_start(b"a\r\n  b\nc\n\n 1 2 3") == 11
+    assert cm.text_data_start(b"a\nb\nc\n1 2 3", header_lines=0) == 0
+
+
+def test_transform_tool_usage(lib, tmp_path):
+    """Usage errors print the reference's message and exit 0 (transform.cpp:11-22)."""
+    exe = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_transform")
+    for argv in ([exe], [exe, str(tmp_path / "missing.txt")], [exe, "a", "b"]):
+        res = subprocess.run(argv, capture_output=True, text=True)
+        assert res.returncode == 0 and res.stdout == "usage: ./transform file_name\n"

@@ -106,3 +106,24 @@ def test_half_rounding_matches_numpy(orc):
         ref = x.astype(np.float16).view(np.uint16)
     got = np.array([orc.lib().or_half_rn(float(v)) for v in x], dtype=np.uint16)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_text_oracle_matches_reference_transform(orc):
+    """The oracle's strict parse reproduces the records the reference's own transform wrote
+    (data/netflix/transform.cpp, compiled from its source) for every text fixture."""
+    z = np.load(os.path.join(GOLDEN, "text.npz"))
+    names = [k[5:] for k in z.files if k.startswith("text_")]
+    assert len(names) >= 8
+    for name in names:
+        got = orc.parse_text(z["text_" + name].tobytes())
+        assert not isinstance(got, tuple), (name, got)
+        assert got.tobytes() == z["bin_" + name].tobytes(), name
+
+
+def test_text_oracle_rejects_malformed_tokens(orc):
+    head = b"a\nb\nc\n"
+    assert orc.parse_text(head + b"1 2 3\n4 5 x\n") == ("bad", len(head) + 10)
+    assert orc.parse_text(head + b"1 2.5 3\n") == ("bad", len(head) + 2)
+    assert orc.parse_text(head + b"1 2 0x1p3\n") == ("bad", len(head) + 4)
+    assert orc.parse_text(head + b"99999999999 2 3\n") == ("bad", len(head))
+    assert orc.parse_text(head + b"1 2 3 4\n") == ("partial", None)
