@@ -46,7 +46,7 @@ def random_text(n, seed):
     fmts = ["%d", "%.1f", "%.9g", "%.17g", "%.6e", "%.18e"]
     seps = [" ", "\t", "  "]
     ends = ["\n", "\r\n", " \n"]
-    out = ["%%MatrixMarket matrix coordinate real general\n%\n2000000 20000 %d\n" % n]
+    out = ["%%%%MatrixMarket matrix coordinate real general\n%%\n2000000 20000 %d\n" % n]
     for i in range(n):
         f = fmts[kind[i]]
         rv = ("%d" % r[i]) if f == "%d" else (f % r[i])
