@@ -6,7 +6,8 @@
 // dW = dY^T X, given as TN products on transposed copies).  One CTA of 128 threads computes a
 // 128 x BN tile (BN = 128 or 256):
 //   - thread 0 is the TMA producer: operand tiles of 64 K-elements (128-byte rows) arrive by
-//     cp.async.bulk.tensor.2d with the 128-byte swizzle into a 4-stage ring of shared memory,
+//     cp.async.bulk.tensor.2d with the 128-byte swizzle into a ring of shared memory (2 stages
+//     for K <= 1024, so two or three CTAs share an SM; 4 stages for longer K),
 //     each stage guarded by a `full` mbarrier (armed with the expected byte count) and an
 //     `empty` mbarrier;
 //   - thread 32 issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=BN, K=16) four times per
@@ -70,7 +71,6 @@ __device__ __forceinline__ float gelu(float x) {
     return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
 }
 
-constexpr int kStages = 4;
 
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
@@ -161,7 +161,7 @@ __device__ __forceinline__ void store_chunk(const uint32_t (&r)[32], int row, in
     }
 }
 
-template <int BN>
+template <int BN, int kStages>
 struct TmaSmem {
     static constexpr int A_BYTES = kTcBM * 128;  // 128 rows x 64 bf16
     static constexpr int B_BYTES = BN * 128;
@@ -169,12 +169,12 @@ struct TmaSmem {
     static constexpr int TOTAL = 1024 + kStages * STAGE + 256;  // alignment slack + barriers
 };
 
-template <int BN>
+template <int BN, int kStages>
 __global__ void __launch_bounds__(kTcThreads, 1)
 tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
                    int N, int K, const float *__restrict__ bias, int act, void *out, int out_f32, int ldo,
                    float *pre_out, int *status, int splits) {
-    using S = TmaSmem<BN>;
+    using S = TmaSmem<BN, kStages>;
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;  // swizzle atoms need 1024-byte alignment
@@ -333,6 +333,18 @@ bool make_map(CUtensorMap *map, const void *ptr, int rows, int K, int box_rows) 
 
 }  // namespace
 
+template <int BN, int ST>
+cudaError_t launch_variant(dim3 grid, const CUtensorMap &ma, const CUtensorMap &mb, int M, int N, int K,
+                           const float *bias, int act, void *out, int out_f32, int ldo, float *pre_out, int *status,
+                           int splits, cudaStream_t s) {
+    const int sm = TmaSmem<BN, ST>::TOTAL;
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    tc_gemm_tma_kernel<BN, ST><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
+                                                            status, splits);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, const float *bias, int act,
                            void *out, int out_f32, int ldo, float *pre_out, int *status, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0 || (K % 8) != 0) return cudaErrorInvalidValue;
@@ -343,29 +355,30 @@ cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, co
     if (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, BN)) return cudaErrorInvalidValue;
     const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + BN - 1) / BN;
     const int kt = (K + kTcBK - 1) / kTcBK;
-    // Split K when the output has too few tiles to fill the GPU and K is long (weight gradients).
+    // Short K (at most 16 stages of 64): a 2-stage ring, so two or three CTAs share an SM and
+    // one CTA's epilogue overlaps another's loads.  Long K: a 4-stage ring, one CTA per SM.
+    const bool short_k = kt <= 16;
+    // Split K when the output has too few tiles to fill the GPU and K is long (weight
+    // gradients): about one wave of CTAs, each with at least 8 stages.
     int splits = 1;
     const bool plain = out_f32 && !bias && act == 0 && !pre_out;
-    if (plain && tiles_m * tiles_n < 152 && kt >= 16) {
-        splits = std::min(kt / 8, std::max(1, 2 * 152 / (tiles_m * tiles_n)));
-        cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
-        if (e != cudaSuccess) return e;
+    if (plain && !short_k && tiles_m * tiles_n < 152) {
+        splits = std::max(1, std::min(kt / 8, 152 / (tiles_m * tiles_n)));
+        if (splits > 1) {
+            cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
+            if (e != cudaSuccess) return e;
+        }
     }
     const dim3 grid(tiles_m, tiles_n, splits);
-    if (wide) {
-        const int sm = TmaSmem<256>::TOTAL;
-        cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        if (e != cudaSuccess) return e;
-        tc_gemm_tma_kernel<256><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
-                                                             status, splits);
-    } else {
-        const int sm = TmaSmem<128>::TOTAL;
-        cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        if (e != cudaSuccess) return e;
-        tc_gemm_tma_kernel<128><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
-                                                             status, splits);
-    }
-    return cudaGetLastError();
+    if (wide)
+        return short_k ? launch_variant<256, 2>(grid, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status,
+                                                splits, s)
+                       : launch_variant<256, 4>(grid, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status,
+                                                splits, s);
+    return short_k ? launch_variant<128, 2>(grid, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status,
+                                            splits, s)
+                   : launch_variant<128, 4>(grid, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status,
+                                            splits, s);
 }
 
 }  // namespace cumf

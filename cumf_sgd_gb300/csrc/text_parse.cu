@@ -393,7 +393,7 @@ __device__ uint32_t parse_float(const unsigned char *t, int64_t i, int64_t len, 
 
 __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned char *__restrict__ t, int64_t start,
                                                            int64_t len, const unsigned long long *block_base,
-                                                           uint32_t *out_words, unsigned long long n_tokens,
+                                                           uint32_t *out_words, unsigned long long cap_tokens,
                                                            unsigned long long *bad) {
     const int64_t seg = ((int64_t)blockIdx.x * kTB + threadIdx.x) * kSeg;
     uint64_t starts = start_mask(t, seg, start, len);
@@ -417,19 +417,16 @@ __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned cha
         starts &= starts - 1;
         const int64_t i = seg + j;
         uint32_t reason = 0, word = 0;
-        if (tok < n_tokens) {
-            const unsigned long long field = tok % 3ull;
-            if (field < 2) {
-                int32_t v = 0;
-                reason = parse_int(t, i, len, &v);
-                word = (uint32_t)v;
-            } else {
-                float f = 0.f;
-                reason = parse_float(t, i, len, &f);
-                word = __float_as_uint(f);
-            }
-            if (reason == 0) out_words[tok] = word;
+        if (tok % 3ull < 2) {
+            int32_t v = 0;
+            reason = parse_int(t, i, len, &v);
+            word = (uint32_t)v;
+        } else {
+            float f = 0.f;
+            reason = parse_float(t, i, len, &f);
+            word = __float_as_uint(f);
         }
+        if (reason == 0 && tok < cap_tokens) out_words[tok] = word;
         if (reason != 0) atomicMin(bad, ((unsigned long long)i << 8) | reason);
         ++tok;
     }
@@ -453,6 +450,15 @@ struct DevBuf {
     }
 };
 
+struct StreamBuf {
+    cudaStream_t s;
+    void *p = nullptr;
+    explicit StreamBuf(cudaStream_t st) : s(st) {}
+    ~StreamBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
 }  // namespace
 
 // Offset of the first byte after `lines` header lines, as fscanf(f, "%[^\n]\n", line) called
@@ -471,41 +477,45 @@ int64_t text_data_start(const unsigned char *p, int64_t len, int lines) {
 // Parses the device text into records.  d_out == NULL (or cap too small) returns the count only.
 int parse_text_device(const unsigned char *d_text, int64_t len, int64_t start, cumf_node *d_out, int64_t cap,
                       int64_t *n_records, cudaStream_t s) {
-    if (!n_records || len < 0 || start < 0 || (len > 0 && !d_text)) return fail(CUMF_ERR_ARG, "parse_text: bad arguments");
+    if (!n_records || len < 0 || start < 0 || cap < 0 || (len > 0 && !d_text))
+        return fail(CUMF_ERR_ARG, "parse_text: bad arguments");
     if (reinterpret_cast<uintptr_t>(d_text) & 15u) return fail(CUMF_ERR_ARG, "parse_text: text must be 16-byte aligned");
     *n_records = 0;
     if (start >= len) return CUMF_OK;
     const int64_t nb = (len + kBlockBytes - 1) / kBlockBytes;
     if (nb > 0x7fffffffll) return fail(CUMF_ERR_ARG, "parse_text: text too large");
-    DevBuf scratch;
-    CUMF_CUDA(cudaMalloc(&scratch.p, (size_t)(nb + 2) * sizeof(unsigned long long)));
+    // Stream-ordered scratch: block counts, then the total, then the first-bad word.
+    StreamBuf scratch(s);
+    CUMF_CUDA(cudaMallocAsync(&scratch.p, (size_t)(nb + 2) * sizeof(unsigned long long), s));
     unsigned long long *counts = static_cast<unsigned long long *>(scratch.p);
     unsigned long long *bad = counts + nb + 1;
     count_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts);
     scan_blocks_kernel<<<1, kScanThreads, 0, s>>>(counts, nb);
     CUMF_CUDA(cudaGetLastError());
-    unsigned long long total = 0;
-    CUMF_CUDA(cudaMemcpyAsync(&total, counts + nb, sizeof(total), cudaMemcpyDeviceToHost, s));
+    unsigned long long tail[2] = {0, ~0ull};  // total tokens, first bad token
+    if (d_out) {
+        // Parse in the same pass; records past `cap` are parsed (for errors) but not stored.
+        CUMF_CUDA(cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), s));
+        parse_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts,
+                                                         reinterpret_cast<uint32_t *>(d_out),
+                                                         (unsigned long long)cap * 3ull, bad);
+        CUMF_CUDA(cudaGetLastError());
+        CUMF_CUDA(cudaMemcpyAsync(tail, counts + nb, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    } else {
+        CUMF_CUDA(cudaMemcpyAsync(tail, counts + nb, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    }
     CUMF_CUDA(cudaStreamSynchronize(s));
+    const unsigned long long total = tail[0];
     if (total % 3 != 0)
         return fail(CUMF_ERR_FORMAT, "parse_text: " + std::to_string(total) +
                                          " tokens do not form whole (u, v, r) records");
     *n_records = (int64_t)(total / 3);
-    if (!d_out || cap < *n_records) {
-        if (d_out) return fail(CUMF_ERR_ARG, "parse_text: output holds " + std::to_string(cap) + " records, " +
-                                                 std::to_string(*n_records) + " needed");
-        return CUMF_OK;
-    }
-    CUMF_CUDA(cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), s));
-    parse_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts, reinterpret_cast<uint32_t *>(d_out),
-                                                     total, bad);
-    CUMF_CUDA(cudaGetLastError());
-    unsigned long long first_bad = 0;
-    CUMF_CUDA(cudaMemcpyAsync(&first_bad, bad, sizeof(first_bad), cudaMemcpyDeviceToHost, s));
-    CUMF_CUDA(cudaStreamSynchronize(s));
-    if (first_bad != ~0ull)
-        return fail(CUMF_ERR_FORMAT, "parse_text: byte " + std::to_string(first_bad >> 8) + ": " +
-                                         reason_text((uint32_t)(first_bad & 0xffu)));
+    if (tail[1] != ~0ull)
+        return fail(CUMF_ERR_FORMAT, "parse_text: byte " + std::to_string(tail[1] >> 8) + ": " +
+                                         reason_text((uint32_t)(tail[1] & 0xffu)));
+    if (d_out && cap < *n_records)
+        return fail(CUMF_ERR_ARG, "parse_text: output holds " + std::to_string(cap) + " records, " +
+                                      std::to_string(*n_records) + " needed");
     return CUMF_OK;
 }
 
