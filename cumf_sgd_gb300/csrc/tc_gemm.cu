@@ -3,19 +3,21 @@
 //   C[M x N] = act(A[M x K] * B[N x K]^T + bias[N])       (A, B bf16 row-major; fp32 accumulate)
 //
 // Used by the warm-start MLP (forward: activations x W^T; backward: dX = dY W and
-// dW = dY^T X, given as TN products on transposed copies).  One CTA of 128 threads computes a
+// dW = dY^T X, given as TN products on transposed copies).  One CTA of 256 threads computes a
 // 128 x BN tile (BN = 128 or 256):
 //   - thread 0 is the TMA producer: operand tiles of 64 K-elements (128-byte rows) arrive by
 //     cp.async.bulk.tensor.2d with the 128-byte swizzle into a ring of shared memory (2 stages
-//     for K <= 1024, so two or three CTAs share an SM; 4 stages for longer K),
+//     for K <= 1024, so two CTAs share an SM; 4 stages for longer K),
 //     each stage guarded by a `full` mbarrier (armed with the expected byte count) and an
 //     `empty` mbarrier;
 //   - thread 32 issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=BN, K=16) four times per
 //     stage, accumulating in tensor memory (BN fp32 columns from tcgen05.alloc), and
 //     tcgen05.commit releases the stage to the producer through `empty`;
-//   - after the last stage a commit to `done` releases the epilogue, in which all four warps
-//     read the accumulator with tcgen05.ld (32 lanes x 32 columns per warp), add the bias,
-//     apply the activation and write 16-byte vectors of bf16 or fp32;
+//   - after the last stage a commit to `done` releases the epilogue: eight warps read the
+//     accumulator with tcgen05.ld (warp w: lanes 32 (w % 4).., half w / 4 of the columns, 32
+//     columns at a time), add the bias, apply the activation, and pass each 32 x 32 block
+//     through shared memory (the idle operand ring) so that the global stores are whole
+//     128-byte lines;
 //   - when the output has too few tiles to fill the GPU and K is long (the weight gradients),
 //     K is split over grid.z and the partial tiles are added into a zeroed fp32 output with
 //     vector atomics.
@@ -36,7 +38,8 @@ namespace cumf {
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;  // 8 warps: all read the accumulator in the epilogue
+constexpr int kStgStride = 36;    // floats per staged row (144 bytes: 16-byte aligned, conflict-free)
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;
 constexpr long long kSpinLimit = 1ll << 24;  // try_wait polls before giving up (seconds)
@@ -89,75 +92,105 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-// Writes 32 consecutive accumulator columns of one output row (col0 .. col0+31, clipped at N):
-// fp32 partial sums by atomics (split K), or bias + activation into fp32 / bf16, with the
-// pre-activation copy when asked.  Whole in-range chunks on 16-byte aligned rows use vectors.
-__device__ __forceinline__ void store_chunk(const uint32_t (&r)[32], int row, int col0, int N,
-                                            const float *__restrict__ bias, int act, void *out, int out_f32,
-                                            int ldo, float *pre_out, bool partial) {
+// Epilogue of one warp's 32 rows x 32 columns (rows r0.., columns col0..; lane = row in r[]):
+// the values pass through shared memory (stg, 32 x kStgStride floats) so that the global
+// stores are whole 128-byte lines per 8 lanes (fp32) or 64-byte segments per 4 lanes (bf16).
+// partial: fp32 partial sums added with vector atomics (split K), no bias or activation.
+__device__ __forceinline__ void stage_f32(float *stg, const float (&v)[32], int lane) {
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<float4 *>(stg + lane * kStgStride + 4 * q) =
+            make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    __syncwarp();
+}
+
+__device__ __forceinline__ void write_f32(const float *stg, float *dst, int r0, int col0, int M, int N, int ldo,
+                                          bool vec_ok, bool atomic, int lane) {
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+        const int row = it * 4 + (lane >> 3), c = (lane & 7) * 4;
+        const int gr = r0 + row, col = col0 + c;
+        if (gr >= M || col >= N) continue;
+        const float4 x = *reinterpret_cast<const float4 *>(stg + row * kStgStride + c);
+        float *o = dst + (size_t)gr * ldo + col;
+        if (vec_ok && col + 3 < N) {
+            if (atomic)
+                atomicAdd(reinterpret_cast<float4 *>(o), x);
+            else
+                *reinterpret_cast<float4 *>(o) = x;
+        } else {
+            const float xs[4] = {x.x, x.y, x.z, x.w};
+            for (int e = 0; e < 4 && col + e < N; ++e) {
+                if (atomic)
+                    atomicAdd(o + e, xs[e]);
+                else
+                    o[e] = xs[e];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void write_bf16(float *stg, const float (&v)[32], __nv_bfloat16 *dst, int r0, int col0,
+                                           int M, int N, int ldo, bool vec_ok, int lane) {
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint4 w;
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
+        *reinterpret_cast<uint4 *>(stg + lane * kStgStride + 4 * q) = w;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+        const int row = it * 8 + (lane >> 2), c = (lane & 3) * 8;
+        const int gr = r0 + row, col = col0 + c;
+        if (gr >= M || col >= N) continue;
+        const uint4 x = *reinterpret_cast<const uint4 *>(stg + row * kStgStride + (lane & 3) * 4);
+        __nv_bfloat16 *o = dst + (size_t)gr * ldo + col;
+        if (vec_ok && col + 7 < N) {
+            *reinterpret_cast<uint4 *>(o) = x;
+        } else {
+            const __nv_bfloat16 *xs = reinterpret_cast<const __nv_bfloat16 *>(&x);
+            for (int e = 0; e < 8 && col + e < N; ++e) o[e] = xs[e];
+        }
+    }
+}
+
+__device__ __forceinline__ void epilogue_chunk(float *stg, const uint32_t (&r)[32], int r0, int col0, int M, int N,
+                                               const float *__restrict__ bias, int act, void *out, int out_f32,
+                                               int ldo, float *pre_out, bool partial, int lane) {
     float v[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-    const bool whole = col0 + 32 <= N;
-    const size_t off = (size_t)row * ldo + col0;
+    const bool al16 = (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
     if (partial) {
-        float *o = reinterpret_cast<float *>(out) + off;
-        if (whole && (ldo & 3) == 0) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 4) atomicAdd(reinterpret_cast<float4 *>(o + j), make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]));
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (col0 + j < N) atomicAdd(o + j, v[j]);
-        }
+        stage_f32(stg, v, lane);
+        write_f32(stg, reinterpret_cast<float *>(out), r0, col0, M, N, ldo, al16 && (ldo & 3) == 0, true, lane);
         return;
     }
     if (bias) {
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-            if (col0 + j < N) v[j] += bias[col0 + j];
+            if (col0 + j < N) v[j] += __ldg(bias + col0 + j);
     }
     if (pre_out) {
-        float *o = pre_out + off;
-        if (whole && (ldo & 3) == 0) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (col0 + j < N) o[j] = v[j];
-        }
+        stage_f32(stg, v, lane);
+        write_f32(stg, pre_out, r0, col0, M, N, ldo,
+                  (reinterpret_cast<uintptr_t>(pre_out) & 15u) == 0 && (ldo & 3) == 0, false, lane);
     }
     if (act == 1) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = gelu(v[j]);
     }
     if (out_f32) {
-        float *o = reinterpret_cast<float *>(out) + off;
-        if (whole && (ldo & 3) == 0) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (col0 + j < N) o[j] = v[j];
-        }
+        stage_f32(stg, v, lane);
+        write_f32(stg, reinterpret_cast<float *>(out), r0, col0, M, N, ldo, al16 && (ldo & 3) == 0, false, lane);
     } else {
-        __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + off;
-        if (whole && (ldo & 7) == 0) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 8) {
-                uint4 w;
-                __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) h[q] = __floats2bfloat162_rn(v[j + 2 * q], v[j + 2 * q + 1]);
-                *reinterpret_cast<uint4 *>(o + j) = w;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (col0 + j < N) o[j] = __float2bfloat16_rn(v[j]);
-        }
+        write_bf16(stg, v, reinterpret_cast<__nv_bfloat16 *>(out), r0, col0, M, N, ldo, al16 && (ldo & 7) == 0,
+                   lane);
     }
 }
 
@@ -170,7 +203,7 @@ struct TmaSmem {
 };
 
 template <int BN, int kStages>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, kStages == 2 ? 2 : 1)
 tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
                    int N, int K, const float *__restrict__ bias, int act, void *out, int out_f32, int ldo,
                    float *pre_out, int *status, int splits) {
@@ -272,10 +305,14 @@ tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_const
         }
     } else if (KT > 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const int row = m0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < BN; c0 += 32) {
+        // Warp w reads tensor-memory lanes 32 (w % 4).. (its rows) and half w / 4 of the
+        // columns.  The operand ring is idle now and holds each warp's staging block.
+        float *stg = reinterpret_cast<float *>(smem_raw + (base - raw)) + warp * (32 * kStgStride);
+        const int quarter = warp & 3, half = warp >> 2;
+        const int r0 = m0 + quarter * 32;
+        for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2) && n0 + c0 < N; c0 += 32) {
             uint32_t r[32];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
                 "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
@@ -287,8 +324,7 @@ tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_const
                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            const int col0 = n0 + c0;
-            if (row < M && col0 < N) store_chunk(r, row, col0, N, bias, act, out, out_f32, ldo, pre_out, splits > 1);
+            epilogue_chunk(stg, r, r0, n0 + c0, M, N, bias, act, out, out_f32, ldo, pre_out, splits > 1, lane);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -355,7 +391,7 @@ cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, co
     if (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, BN)) return cudaErrorInvalidValue;
     const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + BN - 1) / BN;
     const int kt = (K + kTcBK - 1) / kTcBK;
-    // Short K (at most 16 stages of 64): a 2-stage ring, so two or three CTAs share an SM and
+    // Short K (at most 16 stages of 64): a 2-stage ring, so two CTAs share an SM and
     // one CTA's epilogue overlaps another's loads.  Long K: a 4-stage ring, one CTA per SM.
     const bool short_k = kt <= 16;
     // Split K when the output has too few tiles to fill the GPU and K is long (weight
