@@ -309,6 +309,19 @@ def calc_rmse(prob: MFProblem, model: MFModel) -> float:
     return out.value
 
 
+EVAL_CRITERIA = {"rmse": 0, "mae": 1, "gkl": 2, "logloss": 5, "accuracy": 6, "row_mpr": 10, "col_mpr": 11,
+                 "row_auc": 12, "col_auc": 13}
+
+
+def evaluate(prob: MFProblem, model: MFModel, criterion) -> float:
+    """mf-predict -e <criterion> (test/mf.cpp:3841-4044) on the GPU; criterion is LIBMF's
+    number or a name of EVAL_CRITERIA."""
+    c = EVAL_CRITERIA[criterion] if isinstance(criterion, str) else int(criterion)
+    out = C.c_double()
+    _lib.check(_lib.load().cumf_evaluate(C.byref(prob._c), C.byref(model._c), c, C.byref(out)))
+    return out.value
+
+
 def lr_schedule(alpha: float, beta: float, lrate: float, n: int) -> np.ndarray:
     """Learning-rate table of singleGPU/sgd_kernel.cu:144-149."""
     out = np.zeros(n, dtype=np.float32)

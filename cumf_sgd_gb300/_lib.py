@@ -94,6 +94,7 @@ _SIGS = {
     "cumf_parse_args": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Args)]),
     "cumf_read_problem": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Problem)]),
     "cumf_write_problem": (C.c_int, [C.c_char_p, C.POINTER(Problem)]),
+    "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),
     "cumf_text_data_start": (C.c_int, [C.c_char_p, C.c_int64, C.c_int, C.POINTER(C.c_int64)]),

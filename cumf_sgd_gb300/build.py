@@ -3,7 +3,7 @@
 Outputs (all git-ignored, rebuilt on every machine):
   cumf_sgd_gb300/lib/libcumf_sgd.so   the C-ABI library (CUDA kernels for sm_103a + host code)
   cumf_sgd_gb300/bin/cumf_sgd         drop-in for singleGPU/cumf_sgd (main.cpp)
-  cumf_sgd_gb300/bin/cumf_predict     RMSE evaluator (mf-predict -e 0)
+  cumf_sgd_gb300/bin/cumf_predict     evaluator (mf-predict -e 0/1/2/5/6/10-13)
   cumf_sgd_gb300/bin/cumf_transform   rating text -> binary records (data/netflix/transform)
 Translation units compile in parallel; nothing here needs cmake.
 """
@@ -36,6 +36,7 @@ LIB_SOURCES = [
     "mlp.cu",
     "batch.cu",
     "text_parse.cu",
+    "eval.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp", "cumf_transform": "transform_main.cpp"}
 

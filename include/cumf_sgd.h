@@ -11,6 +11,8 @@
  *   singleGPU/main.cpp:33      parse_argument(int, char**)                -> cumf_parse_args
  *   test/mf.cpp:3706           mf_load_model(char const*)                 -> cumf_load_model
  *   test/mf.cpp:3815           calc_rmse(mf_problem*, mf_model*)          -> cumf_rmse
+ *   test/mf.cpp:3841-4044      calc_mae/gkl/logloss/accuracy/mpr/auc      -> cumf_evaluate
+ *   data/netflix/transform.cpp ./transform file_name                      -> cumf_convert_text
  *
  * Conventions (differences from the reference are deliberate and listed here):
  *   - every call returns an int status (CUMF_OK == 0); nothing calls exit().  The message of
@@ -223,6 +225,21 @@ int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params
  * squared error rounded to fp32 and summed in fp64; ids outside the model or a NaN dot
  * predict model->b (mf.cpp:3794-3813). */
 int cumf_rmse(const cumf_problem *te, const cumf_model *model, double *out);
+
+/* Evaluation criteria of mf-predict -e (test/mf-predict.cpp:21-35; test/mf.cpp:3841-4044), on
+ * the GPU: CUMF_EVAL_RMSE (0, same as cumf_rmse), MAE (1), GKL (2), LOGLOSS (5), ACCURACY (6),
+ * ROW_MPR (10), COL_MPR (11), ROW_AUC (12), COL_AUC (13).  Positives for LOGLOSS, ACCURACY,
+ * MPR and AUC are ratings r > 0, as in the reference.  MPR / AUC predict every (row, column)
+ * of the rows that hold a positive (rows x max(te->n, model->n) dot products); test ids must
+ * lie inside [0, max(te->m, model->m)) x [0, max(te->n, model->n)) (CUMF_ERR_RANGE otherwise;
+ * the reference indexes out of bounds).  A set with no qualifying row gives NaN (0 / 0) as
+ * the reference does.  Unknown criteria fail with CUMF_ERR_ARG ("unknown evaluation
+ * criterion", mf-predict.cpp:64). */
+enum {
+    CUMF_EVAL_RMSE = 0, CUMF_EVAL_MAE = 1, CUMF_EVAL_GKL = 2, CUMF_EVAL_LOGLOSS = 5, CUMF_EVAL_ACC = 6,
+    CUMF_EVAL_ROW_MPR = 10, CUMF_EVAL_COL_MPR = 11, CUMF_EVAL_ROW_AUC = 12, CUMF_EVAL_COL_AUC = 13
+};
+int cumf_evaluate(const cumf_problem *te, const cumf_model *model, int criterion, double *out);
 
 /* ---- device-level entry points (caller-owned device memory) ----------------------- */
 /* The learning-rate table lr[t] = (float)(alpha/(1+beta*t^1.5) + lrate), t < n

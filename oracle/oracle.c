@@ -680,3 +680,118 @@ int64_t or_parse_text(const char *text, int64_t len, int header_lines, or_node *
     if (ntok % 3 != 0) return -2;
     return ntok / 3;
 }
+
+
+/* ---- mf-predict criteria (test/mf.cpp:3794-4044) ------------------------------------------ */
+
+/* mf_predict (mf.cpp:3794-3812): sequential float inner product; b out of range or NaN. */
+static float or_predict(const float *P, int32_t m, const float *Q, int32_t n, int k, float b, int32_t u, int32_t v) {
+    if (u < 0 || u >= m || v < 0 || v >= n) return b;
+    const float *p = P + (int64_t)u * k, *q = Q + (int64_t)v * k;
+    float z = 0.f;
+    for (int t = 0; t < k; ++t) z = fmaf(p[t], q[t], z);
+    return isnan(z) ? b : z;
+}
+
+typedef struct { int32_t row, col; float r; } or_rc;
+static int or_cmp_rc(const void *a, const void *b) {
+    const or_rc *x = (const or_rc *)a, *y = (const or_rc *)b;
+    if (x->row != y->row) return x->row < y->row ? -1 : 1;
+    if (x->col != y->col) return x->col < y->col ? -1 : 1;
+    return 0;
+}
+typedef struct { int32_t col; float pred; } or_cp;
+static int or_cmp_pred(const void *a, const void *b) {
+    const float x = ((const or_cp *)a)->pred, y = ((const or_cp *)b)->pred;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* calc_mpr_auc (mf.cpp:3913-4034). */
+static void or_mpr_auc(const or_node *R, int64_t nnz, int32_t prob_m, int32_t prob_n, const float *P, int32_t pm,
+                       const float *Q, int32_t qn, int k, float b, int transpose, double *mpr, double *auc) {
+    const int32_t m = transpose ? (prob_n > qn ? prob_n : qn) : (prob_m > pm ? prob_m : pm);
+    const int32_t n = transpose ? (prob_m > pm ? prob_m : pm) : (prob_n > qn ? prob_n : qn);
+    or_rc *rc = (or_rc *)malloc((size_t)(nnz ? nnz : 1) * sizeof(or_rc));
+    for (int64_t i = 0; i < nnz; ++i) {
+        rc[i].row = transpose ? R[i].v : R[i].u;
+        rc[i].col = transpose ? R[i].u : R[i].v;
+        rc[i].r = R[i].r;
+    }
+    qsort(rc, (size_t)nnz, sizeof(or_rc), or_cmp_rc);
+    int64_t *cnt = (int64_t *)calloc((size_t)m + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < nnz; ++i) cnt[rc[i].row + 1]++;
+    for (int32_t i = 1; i < m + 1; ++i) cnt[i] += cnt[i - 1];
+    or_cp *row = (or_cp *)malloc((size_t)(n ? n : 1) * sizeof(or_cp));
+    int32_t *index = (int32_t *)malloc((size_t)(nnz ? nnz : 1) * sizeof(int32_t));
+    int64_t total_m = 0, total_pos = 0;
+    double all_mpr = 0, all_auc = 0;
+    for (int32_t i = 0; i < m; ++i) {
+        if (cnt[i + 1] - cnt[i] < 1) continue;
+        for (int32_t j = 0; j < n; ++j) {
+            row[j].col = j;
+            row[j].pred = transpose ? or_predict(P, pm, Q, qn, k, b, j, i) : or_predict(P, pm, Q, qn, k, b, i, j);
+        }
+        int32_t pos = 0;
+        for (int64_t j = cnt[i]; j < cnt[i + 1]; ++j) {
+            if (rc[j].r <= 0) continue;
+            index[pos++] = rc[j].col;
+        }
+        if (n - pos < 1 || pos < 1) continue;
+        total_m++;
+        total_pos += pos;
+        for (int32_t q = 0; q < pos; ++q) { /* swap(row[count], row[index[k]]) (mf.cpp:3995-3999) */
+            const or_cp t = row[q];
+            row[q] = row[index[q]];
+            row[index[q]] = t;
+        }
+        qsort(row, (size_t)pos, sizeof(or_cp), or_cmp_pred);
+        double u_mpr = 0, u_auc = 0;
+        for (int32_t g = pos; g < n; ++g) {
+            if (row[pos - 1].pred <= row[g].pred) {
+                u_mpr += pos;
+                continue;
+            }
+            int32_t left = 0, right = pos - 1;
+            while (left < right) {
+                const int32_t mid = (left + right) / 2;
+                if (row[mid].pred > row[g].pred)
+                    right = mid;
+                else
+                    left = mid + 1;
+            }
+            u_mpr += left;
+            u_auc += pos - left;
+        }
+        all_mpr += u_mpr / (n - pos);
+        all_auc += u_auc / (n - pos) / pos;
+    }
+    *mpr = all_mpr / (double)total_pos;
+    *auc = all_auc / (double)total_m;
+    free(rc);
+    free(cnt);
+    free(row);
+    free(index);
+}
+
+double or_evaluate(const or_node *R, int64_t nnz, int32_t prob_m, int32_t prob_n, const float *P, int32_t m,
+                   const float *Q, int32_t n, int k, float b, int criterion) {
+    if (criterion >= 10 && criterion <= 13) {
+        double mpr = 0, auc = 0;
+        or_mpr_auc(R, nnz, prob_m, prob_n, P, m, Q, n, k, b, criterion == 11 || criterion == 13, &mpr, &auc);
+        return criterion <= 11 ? mpr : auc;
+    }
+    if (criterion != 0 && criterion != 1 && criterion != 2 && criterion != 5 && criterion != 6) return NAN;
+    if (nnz == 0) return 0;
+    double acc = 0;
+    for (int64_t i = 0; i < nnz; ++i) {
+        const float r = R[i].r, z = or_predict(P, m, Q, n, k, b, R[i].u, R[i].v);
+        switch (criterion) {
+            case 0: { const float e = r - z; acc += (double)(e * e); break; }
+            case 1: acc += (double)fabsf(r - z); break;
+            case 2: acc += (double)(r * logf(r / z) - r + z); break;
+            case 5: acc += r > 0 ? log(1.0 + (double)expf(-z)) : log(1.0 + (double)expf(z)); break;
+            default: acc += r > 0 ? (z > 0 ? 1 : 0) : (z < 0 ? 1 : 0); break;
+        }
+    }
+    return criterion == 0 ? sqrt(acc / (double)nnz) : acc / (double)nnz;
+}

@@ -159,6 +159,14 @@ double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t 
 int64_t or_parse_text(const char *text, int64_t len, int header_lines, or_node *out, int64_t cap,
                       int64_t *bad_offset);
 
+/* mf-predict's criteria (test/mf.cpp:3794-4044): 0 RMSE, 1 MAE, 2 GKL, 5 LOGLOSS, 6 ACCURACY,
+ * 10 / 11 row- / column-wise MPR, 12 / 13 row- / column-wise AUC.  prob_m / prob_n are the
+ * test problem's extent (mf_problem::m, n).  float predictions (sequential dot, NaN or
+ * out-of-range ids -> b) and the reference's float / double mix.  Returns NAN for an
+ * unknown criterion. */
+double or_evaluate(const or_node *R, int64_t nnz, int32_t prob_m, int32_t prob_n, const float *P, int32_t m,
+                   const float *Q, int32_t n, int k, float b, int criterion);
+
 #ifdef __cplusplus
 }
 #endif

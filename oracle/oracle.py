@@ -121,6 +121,9 @@ def lib() -> C.CDLL:
         _lib.or_calc_rmse_f64.restype = C.c_double
         _lib.or_calc_rmse_f64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                           C.c_int, C.c_double]
+        _lib.or_evaluate.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                     C.c_void_p, C.c_int32, C.c_int, C.c_float, C.c_int]
+        _lib.or_evaluate.restype = C.c_double
         _lib.or_parse_text.argtypes = [C.c_char_p, C.c_int64, C.c_int, C.c_void_p, C.c_int64,
                                         C.POINTER(C.c_int64)]
         _lib.or_parse_text.restype = C.c_int64
@@ -332,3 +335,31 @@ def ref_transform(text: bytes, tmpdir: str) -> bytes:
     subprocess.run([exe, path], check=True, capture_output=True)
     with open(path + ".bin", "rb") as f:
         return f.read()
+
+
+def evaluate(records: np.ndarray, P: np.ndarray, Q: np.ndarray, b: float, criterion: int,
+             prob_m: int = 0, prob_n: int = 0) -> float:
+    """mf-predict criterion (test/mf.cpp:3794-4044) of a float model on test records;
+    prob_m / prob_n default to the records' extent (as read_problem sets them)."""
+    rec = np.ascontiguousarray(records)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    Q = np.ascontiguousarray(Q, dtype=np.float32)
+    if len(rec):
+        prob_m = prob_m or int(rec["u"].max()) + 1
+        prob_n = prob_n or int(rec["v"].max()) + 1
+    return lib().or_evaluate(_ptr(rec) if len(rec) else None, len(rec), prob_m, prob_n, _ptr(P), P.shape[0],
+                             _ptr(Q), Q.shape[0], P.shape[1], b, criterion)
+
+
+def ref_criteria(test_path: str, model_path: str) -> dict:
+    """Every criterion computed by the reference's own test/mf.cpp functions (full precision)."""
+    res = subprocess.run([os.path.join(REF_DIR, "ref_rmse"), test_path, model_path, "all"], check=True,
+                         capture_output=True, text=True)
+    out = {}
+    for line in res.stdout.splitlines():
+        if line.startswith("RMSE_FULL"):
+            out[0] = float(line.split()[1])
+        elif line.startswith("CRIT"):
+            _, c, v = line.split()
+            out[int(c)] = float(v)
+    return out

@@ -7,7 +7,9 @@ reference tree is mounted):
   ref_rmse    - test/mf.cpp read_problem + mf_load_model + calc_rmse (full precision)
   mf-predict  - test/mf-predict.cpp "-e 0" output line
   transform   - data/netflix/transform.cpp (rating text -> 12-byte records)
-Usage: python tests/golden/make_golden.py   (rewrites layout_*.npz, rmse.npz and text.npz)
+  ref_rmse    - (with "all") every mf-predict criterion of test/mf.cpp
+Usage: python tests/golden/make_golden.py [text|eval]   (rewrites layout_*.npz, rmse.npz, text.npz
+and eval.npz, or only the named set)
 """
 from __future__ import annotations
 
@@ -85,6 +87,50 @@ def rmse_fixtures(tmp: str) -> None:
                         **{f"{key}{i}": np.asarray(c[key]) for i, c in enumerate(cases) for key in c})
 
 
+EVAL_CRITERIA = (0, 1, 2, 5, 6, 10, 11, 12, 13)
+
+
+def eval_fixtures(tmp: str) -> None:
+    """All mf-predict criteria from the reference's own test/mf.cpp functions: signed ratings
+    (positives are r > 0 for LOGLOSS, ACCURACY, MPR and AUC), ids outside the model, a NaN
+    prediction, duplicate (u, v) pairs and rows that are all positive."""
+    rng = np.random.default_rng(77)
+    out = {}
+    for i, (m, n, k, nnz, nonneg) in enumerate([(40, 30, 8, 600, False), (120, 90, 32, 3000, False),
+                                                (25, 18, 16, 300, True)]):
+        scale = 0.3 if not nonneg else 0.5
+        P = (rng.standard_normal((m, k)) * scale).astype(np.float32)
+        Q = (rng.standard_normal((n, k)) * scale).astype(np.float32)
+        if nonneg:  # positive predictions for GKL
+            P, Q = np.abs(P), np.abs(Q)
+        b = np.float32(0.5)
+        te = np.empty(nnz, dtype=NODE)
+        te["u"] = rng.integers(0, m + 4, nnz)
+        te["v"] = rng.integers(0, n + 3, nnz)
+        te["r"] = rng.integers(1, 6, nnz).astype(np.float32) if nonneg else \
+            rng.choice(np.array([-1, 0, 1, 2, 3.5], dtype=np.float32), nnz)
+        te["u"][:5], te["v"][:5], te["r"][:5] = 2, 3, np.float32(2.0)  # duplicate positives
+        full_u = m + 1  # a row outside the model whose test entries cover most columns
+        cols = np.arange(0, n + 1)
+        extra = np.zeros(len(cols), dtype=NODE)
+        extra["u"], extra["v"], extra["r"] = full_u, cols, np.float32(1.0)
+        te = np.concatenate([te, extra])
+        if i == 1:
+            P[3, 0] = np.nan
+        tpath, mpath = os.path.join(tmp, f"ev{i}.bin"), os.path.join(tmp, f"ev{i}.model")
+        te.tofile(tpath)
+        with open(mpath, "wb") as f:
+            np.array([0, m, n, k], dtype=np.int32).tofile(f)
+            np.array([b], dtype=np.float32).tofile(f)
+            P.tofile(f)
+            Q.tofile(f)
+        crit = oracle.ref_criteria(tpath, mpath)
+        out.update({f"P{i}": P, f"Q{i}": Q, f"b{i}": b, f"te{i}": te,
+                    f"crit{i}": np.array([crit[c] for c in EVAL_CRITERIA])})
+        print("eval case", i, {c: round(crit[c], 6) for c in EVAL_CRITERIA})
+    np.savez_compressed(os.path.join(HERE, "eval.npz"), criteria=np.array(EVAL_CRITERIA), **out)
+
+
 def text_cases() -> dict:
     """Rating texts the reference's transform accepts: MatrixMarket-style headers, integer and
     decimal ratings in many spellings (exact float ties, the float range ends, subnormals,
@@ -142,9 +188,13 @@ def main() -> None:
         if len(sys.argv) > 1 and sys.argv[1] == "text":
             text_fixtures(tmp)
             return
+        if len(sys.argv) > 1 and sys.argv[1] == "eval":
+            eval_fixtures(tmp)
+            return
         layout_fixtures(tmp)
         rmse_fixtures(tmp)
         text_fixtures(tmp)
+        eval_fixtures(tmp)
 
 
 if __name__ == "__main__":

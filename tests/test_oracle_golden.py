@@ -127,3 +127,18 @@ def test_text_oracle_rejects_malformed_tokens(orc):
     assert orc.parse_text(head + b"1 2 0x1p3\n") == ("bad", len(head) + 4)
     assert orc.parse_text(head + b"99999999999 2 3\n") == ("bad", len(head))
     assert orc.parse_text(head + b"1 2 3 4\n") == ("partial", None)
+
+
+def test_criteria_oracle_matches_reference(orc):
+    """Every mf-predict criterion of the oracle against the reference's own test/mf.cpp
+    functions (golden values computed with oracle/_ref/ref_rmse ... all)."""
+    z = np.load(os.path.join(GOLDEN, "eval.npz"))
+    crits = [int(c) for c in z["criteria"]]
+    for i in range(3):
+        te, P, Q, b = z[f"te{i}"], z[f"P{i}"], z[f"Q{i}"], float(z[f"b{i}"])
+        for c, ref in zip(crits, z[f"crit{i}"]):
+            got = orc.evaluate(te, P, Q, b, c)
+            if np.isnan(ref):
+                assert np.isnan(got), (i, c)
+            else:
+                assert abs(got - ref) <= 1e-6 * max(1.0, abs(ref)), (i, c, got, ref)
