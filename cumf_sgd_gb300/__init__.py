@@ -498,6 +498,23 @@ def sgd_train_ex(tr: MFProblem, te: Optional[MFProblem], param: Parameter, init=
     return MFModel(out), stats, rm[:param.num_iters], ms[:param.num_iters]
 
 
+def sgd_train_ckpt(tr: MFProblem, te: Optional[MFProblem], param: Parameter, path: str, every: int = 1,
+                   resume: bool = True, stop_after: int = 0):
+    """sgd_train with checkpoints of the in-HBM factors every `every` epochs to `path`;
+    resume=True continues from a matching checkpoint; stop_after > 0 ends the call once that
+    many epochs are complete.  Returns (model, stats, epochs_done)."""
+    out = _lib.Model()
+    st = _lib.TrainStats()
+    p = param.to_c()
+    ck = _lib.Checkpoint(path=path.encode(), every=every, resume=int(resume), stop_after=stop_after)
+    done = C.c_int32(0)
+    rc = _lib.load().cumf_train_ckpt(C.byref(tr._c), C.byref(te._c) if te is not None else None, C.byref(p),
+                                     C.byref(ck), C.byref(out), C.byref(st), C.byref(done))
+    _lib.check(rc)
+    stats = TrainStats(**{f: getattr(st, f) for f, _ in _lib.TrainStats._fields_ if f != "reserved_"})
+    return MFModel(out), stats, done.value
+
+
 # ---- batched factorizations ------------------------------------------------------------
 
 class Batch:

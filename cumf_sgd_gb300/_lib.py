@@ -54,6 +54,11 @@ class Tuning(C.Structure):
                 ("ring", C.c_int32), ("freeze_q", C.c_int32), ("reserved_", C.c_int32 * 3)]
 
 
+class Checkpoint(C.Structure):
+    _fields_ = [("path", C.c_char_p), ("every", C.c_int32), ("resume", C.c_int32), ("stop_after", C.c_int32),
+                ("reserved_", C.c_int32 * 3)]
+
+
 class Model(C.Structure):
     _fields_ = [("fun", C.c_int32), ("m", C.c_int32), ("n", C.c_int32), ("k", C.c_int32),
                 ("b", C.c_float), ("pinned", C.c_int32),
@@ -94,6 +99,8 @@ _SIGS = {
     "cumf_parse_args": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Args)]),
     "cumf_read_problem": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Problem)]),
     "cumf_write_problem": (C.c_int, [C.c_char_p, C.POINTER(Problem)]),
+    "cumf_train_ckpt": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Checkpoint),
+                                  C.POINTER(Model), C.POINTER(TrainStats), C.POINTER(C.c_int32)]),
     "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),

@@ -79,9 +79,108 @@ struct EpochEval {
     }
 };
 
+// ---- checkpoints (cumf_train_ckpt) ----------------------------------------------------------
+
+struct CkptHeader {
+    char magic[8];
+    int32_t version, k, precision, workers, lanes, num_iters, epochs_done, m, n, tail_epochs, reserved;
+    uint64_t seed;
+    float lambda_p, lambda_q, alpha, beta, lrate, pad;
+    int64_t nnz, tail_start;
+    uint64_t records_digest, bytes_p, bytes_q, payload_digest;
+};
+constexpr char kCkptMagic[8] = {'C', 'U', 'M', 'F', 'C', 'K', 'P', '1'};
+
+struct PinnedHost {
+    void *p = nullptr;
+    ~PinnedHost() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+int payload_digest(const void *d_P, size_t bp, const void *d_Q, size_t bq, unsigned long long *d_dig, cudaStream_t s,
+                   uint64_t *out) {
+    unsigned long long a = 0, b = 0;
+    CUMF_CUDA(launch_digest(d_P, bp, d_dig, s));
+    CUMF_CUDA(cudaMemcpyAsync(&a, d_dig, sizeof(a), cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    CUMF_CUDA(launch_digest(d_Q, bq, d_dig, s));
+    CUMF_CUDA(cudaMemcpyAsync(&b, d_dig, sizeof(b), cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    *out = (uint64_t)a ^ ((uint64_t)b * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull);
+    return CUMF_OK;
+}
+
+int ckpt_write(const char *path, CkptHeader h, const void *d_P, const void *d_Q, unsigned long long *d_dig,
+               cudaStream_t s) {
+    if (int rc = payload_digest(d_P, h.bytes_p, d_Q, h.bytes_q, d_dig, s, &h.payload_digest)) return rc;
+    PinnedHost buf;
+    CUMF_CUDA(cudaMallocHost(&buf.p, h.bytes_p + h.bytes_q + 16));
+    char *hp = static_cast<char *>(buf.p);
+    CUMF_CUDA(cudaMemcpyAsync(hp, d_P, h.bytes_p, cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaMemcpyAsync(hp + h.bytes_p, d_Q, h.bytes_q, cudaMemcpyDeviceToHost, s));
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if (!f) return fail(CUMF_ERR_IO, "cannot open " + tmp + " for writing");
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    ok = ok && fwrite(hp, 1, h.bytes_p + h.bytes_q, f) == h.bytes_p + h.bytes_q;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp.c_str(), path) != 0) {
+        remove(tmp.c_str());
+        return fail(CUMF_ERR_IO, std::string("checkpoint write failed: ") + path);
+    }
+    return CUMF_OK;
+}
+
+// Loads a matching checkpoint into d_P / d_Q; *found = false when the file does not exist.
+int ckpt_read(const char *path, const CkptHeader &want, void *d_P, void *d_Q, unsigned long long *d_dig,
+              cudaStream_t s, int32_t *epochs_done, bool *found) {
+    *found = false;
+    FILE *f = fopen(path, "rb");
+    if (!f) return CUMF_OK;
+    *found = true;
+    CkptHeader h;
+    const bool got = fread(&h, sizeof(h), 1, f) == 1;
+    auto bad = [&](const char *what) {
+        fclose(f);
+        return fail(CUMF_ERR_FORMAT, std::string("checkpoint ") + path + " does not match this run: " + what);
+    };
+    if (!got || memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) return bad("not a checkpoint file");
+    if (h.k != want.k || h.precision != want.precision) return bad("k or precision");
+    if (h.workers != want.workers || h.lanes != want.lanes) return bad("workers or lanes");
+    if (h.seed != want.seed) return bad("seed");
+    if (h.lambda_p != want.lambda_p || h.lambda_q != want.lambda_q || h.alpha != want.alpha || h.beta != want.beta ||
+        h.lrate != want.lrate)
+        return bad("lambda or learning-rate parameters");
+    if (h.m != want.m || h.n != want.n || h.nnz != want.nnz || h.records_digest != want.records_digest)
+        return bad("training ratings");
+    if (h.tail_epochs != want.tail_epochs || h.tail_start != want.tail_start) return bad("fold-in epochs");
+    if (h.bytes_p != want.bytes_p || h.bytes_q != want.bytes_q) return bad("factor sizes");
+    if (h.epochs_done < 0 || h.epochs_done > want.num_iters) return bad("more epochs done than this run has");
+    PinnedHost buf;
+    if (cudaMallocHost(&buf.p, h.bytes_p + h.bytes_q + 16) != cudaSuccess) {
+        fclose(f);
+        cudaGetLastError();
+        return fail(CUMF_ERR_NOMEM, "cannot allocate pinned memory for the checkpoint");
+    }
+    char *hp = static_cast<char *>(buf.p);
+    const bool full = fread(hp, 1, h.bytes_p + h.bytes_q, f) == h.bytes_p + h.bytes_q;
+    fclose(f);
+    if (!full) return fail(CUMF_ERR_FORMAT, std::string("checkpoint ") + path + " is truncated");
+    CUMF_CUDA(cudaMemcpyAsync(d_P, hp, h.bytes_p, cudaMemcpyHostToDevice, s));
+    CUMF_CUDA(cudaMemcpyAsync(d_Q, hp + h.bytes_p, h.bytes_q, cudaMemcpyHostToDevice, s));
+    uint64_t dg = 0;
+    if (int rc = payload_digest(d_P, h.bytes_p, d_Q, h.bytes_q, d_dig, s, &dg)) return rc;
+    if (dg != h.payload_digest) return fail(CUMF_ERR_FORMAT, std::string("checkpoint ") + path + " fails its digest");
+    *epochs_done = h.epochs_done;
+    return CUMF_OK;
+}
+
 int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_params &p,
                  int workers, int lanes, cumf_model *out, cumf_train_stats *st,
-                 const cumf_model *init = nullptr, double *epoch_rmse = nullptr, double *epoch_ms = nullptr) {
+                 const cumf_model *init = nullptr, double *epoch_rmse = nullptr, double *epoch_ms = nullptr,
+                 const cumf_checkpoint *ck = nullptr, int32_t *epochs_done = nullptr) {
     const double t0 = now_ms();
     const int64_t nnz = tr->nnz;
     const int32_t m = tr->m, n = tr->n;
@@ -93,6 +192,14 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     DevBuf d_R, d_part, d_small, d_pmap, d_qmap, d_P, d_Q, d_lr, d_status, d_pf, d_qf;
     CUMF_CUDA(d_R.alloc(std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
     if (nnz) CUMF_CUDA(cudaMemcpyAsync(d_R.p, tr->R, nnz * sizeof(cumf_node), cudaMemcpyHostToDevice, s));
+    const bool use_ck = ck && ck->path && ck->path[0];
+    DevBuf d_dig;
+    unsigned long long records_digest = 0;
+    if (use_ck) {  // fingerprint of the caller's ratings, before they are permuted and scaled
+        CUMF_CUDA(d_dig.alloc(sizeof(unsigned long long)));
+        CUMF_CUDA(launch_digest(d_R.p, (uint64_t)nnz * sizeof(cumf_node), d_dig.as<unsigned long long>(), s));
+        CUMF_CUDA(cudaMemcpyAsync(&records_digest, d_dig.p, sizeof(records_digest), cudaMemcpyDeviceToHost, s));
+    }
 
     // collect_data on the device.
     Prepared pr;
@@ -179,11 +286,50 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(cudaGetDevice(&dev));
     CUMF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const bool one_wave = workers <= resident_workers(k, p.precision, lanes, sms);
-    const int per_launch = (per_epoch || !one_wave || p.tail_epochs > 0) ? 1
-                           : (p.epochs_per_launch > 0 ? p.epochs_per_launch : std::max(1, p.num_iters));
+    int per_launch = (per_epoch || !one_wave || p.tail_epochs > 0) ? 1
+                     : (p.epochs_per_launch > 0 ? p.epochs_per_launch : std::max(1, p.num_iters));
     const bool tail = p.tail_epochs > 0 && p.tail_start > 0 && p.tail_start < nnz;
-    for (int ep = 0; ep < p.num_iters; ep += per_launch) {
-        int cnt = std::min(per_launch, p.num_iters - ep);
+
+    // Checkpoints: resume, then launches that end on multiples of `every`.
+    CkptHeader ckh;
+    memset(&ckh, 0, sizeof(ckh));
+    int first_ep = 0, last_ep = p.num_iters;
+    if (use_ck) {
+        memcpy(ckh.magic, kCkptMagic, 8);
+        ckh.version = 1;
+        ckh.k = k;
+        ckh.precision = p.precision;
+        ckh.workers = workers;
+        ckh.lanes = lanes;
+        ckh.num_iters = p.num_iters;
+        ckh.m = m;
+        ckh.n = n;
+        ckh.tail_epochs = p.tail_epochs;
+        ckh.seed = p.seed;
+        ckh.lambda_p = p.lambda_p;
+        ckh.lambda_q = p.lambda_q;
+        ckh.alpha = p.alpha;
+        ckh.beta = p.beta;
+        ckh.lrate = p.lrate;
+        ckh.nnz = nnz;
+        ckh.tail_start = p.tail_start;
+        ckh.records_digest = records_digest;
+        ckh.bytes_p = (uint64_t)m * k * eb;
+        ckh.bytes_q = (uint64_t)n * k * eb;
+        if (ck->resume) {
+            bool found = false;
+            int32_t done = 0;
+            if (int rc = ckpt_read(ck->path, ckh, d_P.p, d_Q.p, d_dig.as<unsigned long long>(), s, &done, &found))
+                return rc;
+            if (found) first_ep = done;
+        }
+        if (ck->every > 0) per_launch = std::min(per_launch, ck->every);
+        if (ck->stop_after > 0) last_ep = std::min(last_ep, std::max(first_ep, (int)ck->stop_after));
+    }
+    CUMF_CUDA(cudaStreamSynchronize(s));
+    for (int ep = first_ep; ep < last_ep;) {
+        int cnt = std::min(per_launch, last_ep - ep);
+        if (use_ck && ck->every > 0) cnt = std::min(cnt, ck->every - ep % ck->every);
         const cumf_node *R_ep = d_R.as<cumf_node>();
         int64_t nnz_ep = nnz;
         int workers_ep = workers;
@@ -192,8 +338,6 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
             R_ep += p.tail_start;
             nnz_ep = nnz - p.tail_start;
             workers_ep = (int)std::min<int64_t>(workers, std::max<int64_t>(1, nnz_ep / 1024));
-        } else if (tail) {
-            cnt = std::min(cnt, p.num_iters - ep);
         }
         CUMF_CUDA(cudaEventRecord(e0.e, s));
         Tuning tu;
@@ -222,7 +366,14 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
                 fflush(stdout);
             }
         }
+        ep += cnt;
+        if (use_ck && ((ck->every > 0 && ep % ck->every == 0) || ep == last_ep)) {
+            ckh.epochs_done = ep;
+            if (int rc = ckpt_write(ck->path, ckh, d_P.p, d_Q.p, d_dig.as<unsigned long long>(), s)) return rc;
+        }
     }
+    if (epochs_done) *epochs_done = std::max(first_ep, last_ep);
+    const int epochs_run = std::max(0, last_ep - first_ep);
     int status = 0;
     CUMF_CUDA(cudaMemcpyAsync(&status, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     const double t2 = now_ms();
@@ -251,7 +402,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         st->train_ms = train_ms;
         st->export_ms = t3 - t2;
         st->total_ms = t3 - t0;
-        st->updates_per_sec = train_ms > 0 ? (double)nnz * p.num_iters / (train_ms * 1e-3) : 0.0;
+        st->updates_per_sec = train_ms > 0 ? (double)nnz * epochs_run / (train_ms * 1e-3) : 0.0;
         st->samples_per_epoch = (int64_t)workers * batches_per_worker(nnz, workers) * 128;
         st->mean = pr.ave;
         st->std_dev = pr.std_dev;
@@ -260,7 +411,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         st->lanes = lanes_used;
     }
     if (!p.quiet) {
-        printf("update_per_sec:%f\n", train_ms > 0 ? (double)nnz * p.num_iters / (train_ms * 1e-3) : 0.0);
+        printf("update_per_sec:%f\n", train_ms > 0 ? (double)nnz * epochs_run / (train_ms * 1e-3) : 0.0);
         fflush(stdout);
     }
     return CUMF_OK;
@@ -349,6 +500,27 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
     const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
     if (!p.quiet) print_args(p);
     return train_mode_a(tr, te, p, p.num_workers, lanes, out, stats, init, epoch_rmse, epoch_ms);
+}
+
+int cumf_train_ckpt(const cumf_problem *tr, const cumf_problem *te, const cumf_params *params,
+                    const cumf_checkpoint *ckpt, cumf_model *out, cumf_train_stats *stats, int32_t *epochs_done) {
+    if (!tr || !out || !ckpt || !ckpt->path || !ckpt->path[0])
+        return fail(CUMF_ERR_ARG, "train_ckpt: problem, model and checkpoint path must be given");
+    if (ckpt->every < 0 || ckpt->stop_after < 0) return fail(CUMF_ERR_ARG, "train_ckpt: negative every or stop_after");
+    if (tr->nnz < 0 || (tr->nnz > 0 && !tr->R) || tr->m < 1 || tr->n < 1)
+        return fail(CUMF_ERR_ARG, "train_ckpt: malformed problem");
+    memset(out, 0, sizeof(*out));
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (epochs_done) *epochs_done = 0;
+    if (int rc = check_params(params)) return rc;
+    cumf_params p = *params;
+    if (p.u_grid * p.v_grid != 1) return fail(CUMF_ERR_ARG, "train_ckpt: checkpoints need u = v = 1 (the whole problem in HBM)");
+    p.x_grid = p.y_grid = 1;
+    p.ux = p.vy = 1;
+    if (int rc = select_device(p.gpu)) return rc;
+    const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    if (!p.quiet) print_args(p);
+    return train_mode_a(tr, te, p, p.num_workers, lanes, out, stats, nullptr, nullptr, nullptr, ckpt, epochs_done);
 }
 
 int cumf_rmse(const cumf_problem *te, const cumf_model *model, double *out) {

@@ -3,17 +3,50 @@
 //   cumf_sgd [-g id] [-l lp[,lq]] [-k 128] [-t iters] [-r lrate] [-a alpha] [-b beta]
 //            [-s workers] [-u U] [-v V] [-x X] [-y Y] [-p test_file]
 //            [--seed N] [--precision fp16|bf16|fp32|bf16sr|fp16sr] [--lanes N] [--quiet]
+//            [--checkpoint path [--checkpoint-every N] [--resume]]
 //            train_file [model_file]
 //
 // Exit status 1 on bad arguments (main.cpp:286-289); unlike the reference, a failed read,
 // training or model write also exits non-zero with the library's message.  With -p the
 // test RMSE is printed after each epoch (the reference parses -p but never reads it).
+// --checkpoint writes the in-HBM factors every N epochs (default 1; mode A only) and
+// --resume continues from a matching checkpoint (cumf_train_ckpt).
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+
+#include <vector>
 
 #include "cumf_sgd.h"
 
 int main(int argc, char **argv) {
+    // Checkpoint flags are taken out before the reference flags are parsed.
+    cumf_checkpoint ck;
+    memset(&ck, 0, sizeof(ck));
+    ck.every = 1;
+    std::vector<char *> rest;
+    for (int i = 0; i < argc; ++i) {
+        if (strcmp(argv[i], "--checkpoint") == 0 || strcmp(argv[i], "--checkpoint-every") == 0) {
+            if (i + 1 >= argc) {
+                printf("error: %s needs a value\n", argv[i]);
+                return 1;
+            }
+            if (argv[i][12] == '\0')
+                ck.path = argv[++i];
+            else
+                ck.every = atoi(argv[++i]);
+        } else if (strcmp(argv[i], "--resume") == 0) {
+            ck.resume = 1;
+        } else {
+            rest.push_back(argv[i]);
+        }
+    }
+    if ((ck.resume || ck.every != 1) && !ck.path) {
+        printf("error: --resume and --checkpoint-every need --checkpoint\n");
+        return 1;
+    }
+    argc = (int)rest.size();
+    argv = rest.data();
     cumf_args arg;
     if (cumf_parse_args(argc, argv, &arg) != CUMF_OK) {
         printf("%s\n", cumf_last_error());
@@ -37,7 +70,8 @@ int main(int argc, char **argv) {
     }
     cumf_model model;
     cumf_train_stats st;
-    int rc = cumf_train(&tr, have_va ? &va : nullptr, &arg.param, &model, &st);
+    int rc = ck.path ? cumf_train_ckpt(&tr, have_va ? &va : nullptr, &arg.param, &ck, &model, &st, nullptr)
+                     : cumf_train(&tr, have_va ? &va : nullptr, &arg.param, &model, &st);
     if (rc != CUMF_OK) {
         printf("training failed: %s\n", cumf_last_error());
         cumf_free_problem(&tr);

@@ -74,6 +74,9 @@ cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, 
                              const float *Q, int32_t n, int k, float b, int blocks,
                              double *d_part, double *d_sum, cudaStream_t s);
 
+// Order-independent digest of `bytes` (a multiple of 4) at d into *d_out.
+cudaError_t launch_digest(const void *d, uint64_t bytes, unsigned long long *d_out, cudaStream_t s);
+
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }
 

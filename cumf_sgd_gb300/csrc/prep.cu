@@ -188,7 +188,26 @@ int grid_for(uint64_t items, int per_thread = 1) {
     return (int)blocks;
 }
 
+// Order-independent 64-bit digest of a byte buffer (a multiple of 4 bytes): the sum of
+// splitmix64(word, index) over its 32-bit words.
+__global__ void digest_kernel(const uint32_t *w, uint64_t nwords, unsigned long long *out) {
+    unsigned long long acc = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
+        acc += splitmix64(((uint64_t)__ldg(w + i) << 32) ^ (i * 0x9E3779B97F4A7C15ull));
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
 }  // namespace
+
+cudaError_t launch_digest(const void *d, uint64_t bytes, unsigned long long *d_out, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || bytes < 4) return e;
+    const uint64_t words = bytes / 4;
+    digest_kernel<<<grid_for(words, 8), kThreads, 0, s>>>(static_cast<const uint32_t *>(d), words, d_out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_init_factors(void *d, int64_t rows, int k, int precision, uint64_t seed,
                                 uint32_t tag, cudaStream_t s, uint64_t index_offset) {

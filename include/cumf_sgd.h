@@ -375,6 +375,28 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
                   const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
                   double *epoch_ms);
 
+/* ---- checkpoint / resume (no reference counterpart) ---------------------------------- */
+/* Periodic checkpoints of a mode-A run (u = v = 1).  The file holds the factors exactly as
+ * training keeps them in HBM (permuted rows, scaled, storage precision), the number of
+ * completed epochs and a fingerprint of the run (k, precision, workers, lanes, seed,
+ * lambdas, learning-rate parameters, problem extent and a digest of the ratings).
+ * Everything else (id maps, scaling, learning rates, sample draws) is recomputed from the
+ * inputs, so a resumed run continues the same epoch sequence; with one worker (or any
+ * deterministic configuration) it is bit-identical to an uninterrupted run that launches
+ * the same epoch chunks.  Files are written to path + ".tmp" and renamed. */
+typedef struct cumf_checkpoint {
+    const char *path;      /* checkpoint file                                                */
+    int32_t every;         /* write after every `every` completed epochs (0 = at the end)    */
+    int32_t resume;        /* 1 = continue from `path` when it exists (it must match the run) */
+    int32_t stop_after;    /* > 0: stop once this many epochs are complete and return the
+                              model as it is then (an interrupted run); 0 = run all epochs   */
+    int32_t reserved_[3];
+} cumf_checkpoint;
+/* cumf_train_ex with checkpoints: *epochs_done (may be NULL) receives the completed epoch
+ * count.  A checkpoint that does not match the run or fails its digest is CUMF_ERR_FORMAT. */
+int cumf_train_ckpt(const cumf_problem *tr, const cumf_problem *te, const cumf_params *params,
+                    const cumf_checkpoint *ckpt, cumf_model *out, cumf_train_stats *stats, int32_t *epochs_done);
+
 /* ---- batched factorizations (no reference counterpart) ------------------------------ */
 /* One problem of a batch: device ratings with ids in range and ratings already scaled, fp16
  * factors P (m x k) and Q (n x k), k in {32, 64, 128}; num_workers 0 = set by the batch

@@ -203,3 +203,21 @@ def test_transform_tool_usage(lib, tmp_path):
     for argv in ([exe], [exe, str(tmp_path / "missing.txt")], [exe, "a", "b"]):
         res = subprocess.run(argv, capture_output=True, text=True)
         assert res.returncode == 0 and res.stdout == "usage: ./transform file_name\n"
+
+
+def test_checkpoint_arguments_without_gpu(lib, tmp_path):
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import _lib as L
+    prob = cm.MFProblem.from_arrays([0, 1], [0, 1], [1.0, 2.0])
+    with pytest.raises(cm.CumfError) as e:
+        cm.sgd_train_ckpt(prob, None, cm.Parameter(k=128), "", every=1)
+    assert e.value.code == L.CUMF_ERR_ARG
+    with pytest.raises(cm.CumfError) as e:
+        cm.sgd_train_ckpt(prob, None, cm.Parameter(k=128), str(tmp_path / "x"), every=-1)
+    assert e.value.code == L.CUMF_ERR_ARG
+    with pytest.raises(cm.CumfError) as e:
+        cm.sgd_train_ckpt(prob, None, cm.Parameter(k=128, u_grid=2, v_grid=2), str(tmp_path / "x"))
+    assert e.value.code == L.CUMF_ERR_ARG
+    exe = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_sgd")
+    res = subprocess.run([exe, "--resume", "train.bin"], capture_output=True, text=True)
+    assert res.returncode == 1 and "--checkpoint" in res.stdout
