@@ -1,6 +1,7 @@
 // predict_main.cpp - `cumf_predict [-e eval] test_file model_file [output_file]`: LIBMF's
 // mf-predict (test/mf-predict.cpp:15-220) with every criterion evaluated on the GPU.  Output
-// lines, messages and exit codes follow the reference: "RMSE = x.xxxx" (and MAE, GKL,
+// lines, messages and exit codes follow the reference: "calculating rmse ..." and
+// "RMSE = x.xxxx" (and MAE, GKL,
 // LOGLOSS, ACCURACY, Row-wise / Colmn-wise AUC, Row-wise / Column-wise MPR), then
 // "time elapsed:...s"; argument errors print the reference's message and exit 1.
 #include <stdio.h>
@@ -81,6 +82,7 @@ int main(int argc, char **argv) {
         return 1;
     }
     const clock_t start = clock();
+    if (eval == CUMF_EVAL_RMSE) printf("calculating rmse ...\n");  // calc_rmse's line (mf.cpp:3817)
     double v = 0;
     int rc = cumf_evaluate(&te, &model, eval, &v);
     if (rc == CUMF_OK) {

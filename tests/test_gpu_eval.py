@@ -94,6 +94,10 @@ def test_predict_tool_prints_reference_lines(lib, cuda, tmp_path):
             continue
         out = subprocess.run([exe, "-e", str(c), str(tpath), str(mpath)], capture_output=True, text=True)
         assert out.returncode == 0, out.stdout
-        assert out.stdout.splitlines()[0] == labels[c] + "%.4f" % ref
+        lines = out.stdout.splitlines()
+        assert [ln for ln in lines if ln.startswith(labels[c])] == [labels[c] + "%.4f" % ref]
+        assert lines[-1].startswith("time elapsed:")
+        if c == 0:
+            assert lines[0] == "calculating rmse ..."
     out = subprocess.run([exe, "-e", "3", str(tpath), str(mpath)], capture_output=True, text=True)
     assert out.returncode == 1 and out.stdout.strip() == "unknown evaluation criterion"

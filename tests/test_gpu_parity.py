@@ -295,7 +295,7 @@ def test_cli_train_and_predict(lib, orc, cuda, tmp_path):
     res = subprocess.run([os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_predict"), "-e", "0", tep, mp],
                          capture_output=True, text=True)
     assert res.returncode == 0
-    got = float(res.stdout.strip().split("=")[1])
+    got = float([ln for ln in res.stdout.splitlines() if ln.startswith("RMSE = ")][0].split("=")[1])
     m = cm.mf_load_model(mp)
     assert abs(got - orc.calc_rmse(te, m.P, m.Q, m.b)) < 1e-4
 
