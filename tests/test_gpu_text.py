@@ -130,3 +130,33 @@ def test_capacity_errors(lib, cuda):
         cm.dev_parse_text(d.data_ptr(), len(text), 0, out.data_ptr(), 1)
     with pytest.raises(cm.CumfError):  # misaligned text
         cm.dev_parse_text(d.data_ptr() + 1, len(text) - 1, 0)
+
+
+@pytest.mark.parametrize("body,where", [
+    (b"1 2 .e5\n", 4), (b"1 2 1e+\n", 4), (b"1 2 -\n", 4), (b"1 2 +.\n", 4), (b"1 2 1.5e5.5\n", 4),
+    (b"12a 2 3\n", 0), (b"1 - 3\n", 2), (b"1 2 e5\n", 4), (b"1 2 1..\n", 4), (b"3000000000 2 3\n", 0)])
+def test_malformed_short_tokens_mid_text(lib, cuda, orc, tmp_path, body, where):
+    """Short malformed tokens followed by more text: rejected at the oracle's offset."""
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import _lib
+    head = b"a\nb\nc\n"
+    text = head + body + b"7 8 9\n" * 12
+    assert orc.parse_text(text) == ("bad", len(head) + where)
+    p = tmp_path / "bad.txt"
+    p.write_bytes(text)
+    with pytest.raises(cm.CumfError) as e:
+        cm.convert_text(str(p))
+    assert e.value.code == _lib.CUMF_ERR_FORMAT
+    assert "byte %d:" % (len(head) + where) in str(e.value)
+
+
+def test_valid_spellings_mid_text(lib, cuda, orc, tmp_path):
+    import cumf_sgd_gb300 as cm
+    toks = [b"+4", b"007", b"-0.0", b"4.", b".5", b"-.25", b"1e-3", b"2.5E+1", b"5e0", b"0e10", b"16777217",
+            b"0.1", b"3.4e38", b"1e-45", b"inf", b"-nan", b"123456789012345", b"1.25e-07"]
+    body = b"".join(b"%d %d %s\n" % (i, i + 1, t) for i, t in enumerate(toks)) + b"7 8 9\n" * 12
+    text = b"a\nb\nc\n" + body
+    p = tmp_path / "ok.txt"
+    p.write_bytes(text)
+    assert cm.convert_text(str(p)) == len(toks) + 12
+    assert (tmp_path / "ok.txt.bin").read_bytes() == orc.parse_text(text).tobytes()
