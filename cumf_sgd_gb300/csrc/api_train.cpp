@@ -264,7 +264,8 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(cudaMemcpyAsync(d_lr.p, lr.data(), lr.size() * sizeof(float), cudaMemcpyHostToDevice, s));
 
     const float factor = (float)sqrt(pr.scale);  // scale_model (sgd.cu:598)
-    const float b = pr.ave / pr.std_dev;           // model->b (sgd.cu:679)
+    // model->b (sgd.cu:679); an empty problem (0 / 0 in the reference) gets b = 0.
+    const float b = nnz ? pr.ave / pr.std_dev : 0.f;
     EpochEval ev;
     const bool per_epoch = (p.verbose_epochs || epoch_rmse || epoch_ms) && va && va->nnz > 0;
     if (per_epoch) {

@@ -308,7 +308,7 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     // shuffle_model); the model may not fit the device in these modes.
     if (int rc = cumf_alloc_model(m, n, k, out)) return rc;
     const float factor = (float)sqrt(pr.scale);
-    out->b = pr.ave / pr.std_dev;
+    out->b = tr->nnz ? pr.ave / pr.std_dev : 0.f;  // empty problem: b = 0 (0 / 0 in the reference)
     parallel_for(m, [&](int64_t o) {
         const int64_t src = pm[o];
         for (int j = 0; j < k; ++j) out->P[o * k + j] = store_to_float(Ph, src * k + j, p.precision) * factor;
