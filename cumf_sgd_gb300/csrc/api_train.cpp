@@ -177,6 +177,35 @@ int ckpt_read(const char *path, const CkptHeader &want, void *d_P, void *d_Q, un
     return CUMF_OK;
 }
 
+// The output model's host buffers (page-locked: about 10-25 ms for the c2 model) are
+// allocated on a helper thread while the epochs run; the export then only copies.
+struct ModelAlloc {
+    cumf_model model;
+    int rc = CUMF_OK;
+    std::string msg;
+    std::thread th;
+    bool taken = false;
+    void start(int dev, int32_t m, int32_t n, int32_t k) {
+        memset(&model, 0, sizeof(model));
+        th = std::thread([this, dev, m, n, k] {
+            cudaSetDevice(dev);
+            rc = cumf_alloc_model(m, n, k, &model);
+            if (rc) msg = cumf_last_error();
+        });
+    }
+    int take(cumf_model *out) {
+        if (th.joinable()) th.join();
+        if (rc) return fail(rc, msg);
+        *out = model;
+        taken = true;
+        return CUMF_OK;
+    }
+    ~ModelAlloc() {
+        if (th.joinable()) th.join();
+        if (!taken && rc == CUMF_OK) cumf_free_model(&model);
+    }
+};
+
 int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_params &p,
                  int workers, int lanes, cumf_model *out, cumf_train_stats *st,
                  const cumf_model *init = nullptr, double *epoch_rmse = nullptr, double *epoch_ms = nullptr,
@@ -188,6 +217,12 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     Stream stream;
     CUMF_CUDA(cudaStreamCreateWithFlags(&stream.s, cudaStreamNonBlocking));
     cudaStream_t s = stream.s;
+    ModelAlloc model_alloc;
+    {
+        int cur = 0;
+        CUMF_CUDA(cudaGetDevice(&cur));
+        model_alloc.start(cur, m, n, k);
+    }
 
     DevBuf d_R, d_part, d_small, d_pmap, d_qmap, d_P, d_Q, d_lr, d_status, d_pf, d_qf;
     CUMF_CUDA(d_R.alloc(std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
@@ -328,6 +363,10 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         if (ck->stop_after > 0) last_ep = std::min(last_ep, std::max(first_ep, (int)ck->stop_after));
     }
     CUMF_CUDA(cudaStreamSynchronize(s));
+    // Epochs are launched back to back unless an evaluation or a checkpoint needs the factors
+    // between them (a host wait after every epoch measured 14.2 ms per c2 epoch against 12.9).
+    const bool sync_each = per_epoch || use_ck;
+    if (!sync_each) CUMF_CUDA(cudaEventRecord(e0.e, s));
     for (int ep = first_ep; ep < last_ep;) {
         int cnt = std::min(per_launch, last_ep - ep);
         if (use_ck && ck->every > 0) cnt = std::min(cnt, ck->every - ep % ck->every);
@@ -340,7 +379,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
             nnz_ep = nnz - p.tail_start;
             workers_ep = (int)std::min<int64_t>(workers, std::max<int64_t>(1, nnz_ep / 1024));
         }
-        CUMF_CUDA(cudaEventRecord(e0.e, s));
+        if (sync_each) CUMF_CUDA(cudaEventRecord(e0.e, s));
         Tuning tu;
         tu.lanes = lanes;
         tu.prefetch = p.prefetch;
@@ -350,11 +389,13 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m, d_Q.p, n, k, p.precision, workers_ep, tu,
                                     d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
                                     &lanes_used));
-        CUMF_CUDA(cudaEventRecord(e1.e, s));
-        CUMF_CUDA(cudaEventSynchronize(e1.e));
         float ms = 0;
-        CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
-        train_ms += ms;
+        if (sync_each) {
+            CUMF_CUDA(cudaEventRecord(e1.e, s));
+            CUMF_CUDA(cudaEventSynchronize(e1.e));
+            CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
+            train_ms += ms;
+        }
         if (per_epoch) {
             double rmse = 0;
             if (int rc = ev.eval(d_P.p, d_Q.p, p.precision, d_pmap.as<int32_t>(), d_qmap.as<int32_t>(), factor, b, s, &rmse))
@@ -373,6 +414,13 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
             if (int rc = ckpt_write(ck->path, ckh, d_P.p, d_Q.p, d_dig.as<unsigned long long>(), s)) return rc;
         }
     }
+    if (!sync_each) {
+        float ms = 0;
+        CUMF_CUDA(cudaEventRecord(e1.e, s));
+        CUMF_CUDA(cudaEventSynchronize(e1.e));
+        CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
+        train_ms = ms;
+    }
     if (epochs_done) *epochs_done = std::max(first_ep, last_ep);
     const int epochs_run = std::max(0, last_ep - first_ep);
     int status = 0;
@@ -384,7 +432,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(d_qf.alloc((size_t)n * k * sizeof(float)));
     CUMF_CUDA(launch_export(d_P.p, p.precision, d_pmap.as<int32_t>(), m, k, factor, d_pf.as<float>(), s));
     CUMF_CUDA(launch_export(d_Q.p, p.precision, d_qmap.as<int32_t>(), n, k, factor, d_qf.as<float>(), s));
-    if (int rc = cumf_alloc_model(m, n, k, out)) return rc;
+    if (int rc = model_alloc.take(out)) return rc;
     out->b = b;
     cudaError_t ce = cudaMemcpyAsync(out->P, d_pf.p, (size_t)m * k * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(out->Q, d_qf.p, (size_t)n * k * sizeof(float), cudaMemcpyDeviceToHost, s);
