@@ -144,10 +144,11 @@ class MFProblem:
 
     @property
     def records(self) -> np.ndarray:
-        """Zero-copy structured view (u, v, r) of the records."""
+        """Zero-copy structured view (u, v, r) of the records; the view keeps this problem alive."""
         if self._c.nnz == 0:
             return np.zeros(0, dtype=NODE_DTYPE)
         buf = (C.c_char * (12 * self._c.nnz)).from_address(C.addressof(self._c.R.contents))
+        buf._owner = self
         return np.frombuffer(buf, dtype=NODE_DTYPE)
 
     def write(self, path: str) -> None:
@@ -220,9 +221,12 @@ class MFModel:
         return mod
 
     def _view(self, ptr, rows: int) -> np.ndarray:
+        """Zero-copy view of a factor matrix; the view keeps this model (and its buffers) alive."""
         if rows * self._c.k == 0:
             return np.zeros((rows, self._c.k), dtype=np.float32)
-        return np.ctypeslib.as_array(ptr, shape=(rows, self._c.k))
+        buf = (C.c_char * (4 * rows * self._c.k)).from_address(C.addressof(ptr.contents))
+        buf._owner = self
+        return np.frombuffer(buf, dtype=np.float32).reshape(rows, self._c.k)
 
     @property
     def P(self) -> np.ndarray:
