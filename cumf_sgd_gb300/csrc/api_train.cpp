@@ -177,55 +177,6 @@ int ckpt_read(const char *path, const CkptHeader &want, void *d_P, void *d_Q, un
     return CUMF_OK;
 }
 
-// The output model's host buffers are allocated and touched (first-touch page faults cost
-// about 10 ms for the c2 model) on a helper thread that makes no CUDA call, while the epochs
-// run; the export then only copies (pageable memory that has been touched copies as fast
-// as page-locked memory on a host attached to the GPU coherently; page-locking the buffers
-// instead costs 9-24 ms and contends with the training thread's CUDA calls).
-struct ModelAlloc {
-    cumf_model model;
-    bool ok = false;
-    std::thread th;
-    bool taken = false;
-    void start(int32_t m, int32_t n, int32_t k) {
-        memset(&model, 0, sizeof(model));
-        th = std::thread([this, m, n, k] {
-            const size_t pb = (size_t)std::max<int64_t>(1, (int64_t)m * k) * sizeof(float);
-            const size_t qb = (size_t)std::max<int64_t>(1, (int64_t)n * k) * sizeof(float);
-            model.P = static_cast<float *>(malloc(pb));
-            model.Q = static_cast<float *>(malloc(qb));
-            if (!model.P || !model.Q) return;
-            memset(model.P, 0, pb);
-            memset(model.Q, 0, qb);
-            model.pinned = 0;
-            model.m = m;
-            model.n = n;
-            model.k = k;
-            ok = true;
-        });
-    }
-    int take(cumf_model *out) {
-        if (th.joinable()) th.join();
-        if (!ok) {
-            free(model.P);
-            free(model.Q);
-            model.P = model.Q = nullptr;
-            taken = true;
-            return fail(CUMF_ERR_NOMEM, "cannot allocate model");
-        }
-        *out = model;
-        taken = true;
-        return CUMF_OK;
-    }
-    ~ModelAlloc() {
-        if (th.joinable()) th.join();
-        if (!taken) {
-            free(model.P);
-            free(model.Q);
-        }
-    }
-};
-
 int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_params &p,
                  int workers, int lanes, cumf_model *out, cumf_train_stats *st,
                  const cumf_model *init = nullptr, double *epoch_rmse = nullptr, double *epoch_ms = nullptr,
@@ -237,8 +188,6 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     Stream stream;
     CUMF_CUDA(cudaStreamCreateWithFlags(&stream.s, cudaStreamNonBlocking));
     cudaStream_t s = stream.s;
-    ModelAlloc model_alloc;
-    model_alloc.start(m, n, k);
 
     DevBuf d_R, d_part, d_small, d_pmap, d_qmap, d_P, d_Q, d_lr, d_status, d_pf, d_qf;
     CUMF_CUDA(d_R.alloc(std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
@@ -458,7 +407,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     }
     CUMF_CUDA(launch_export(d_P.p, p.precision, d_pmap.as<int32_t>(), m, k, factor, pf, s));
     CUMF_CUDA(launch_export(d_Q.p, p.precision, d_qmap.as<int32_t>(), n, k, factor, qf, s));
-    if (int rc = model_alloc.take(out)) return rc;
+    if (int rc = cumf_alloc_model(m, n, k, out)) return rc;
     out->b = b;
     cudaError_t ce = cudaMemcpyAsync(out->P, pf, pfb, cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(out->Q, qf, qfb, cudaMemcpyDeviceToHost, s);
