@@ -643,6 +643,41 @@ def run_text_suite(args):
                                      "cores": 1, "kind": "port (strtol/strtof)"}}), flush=True)
 
 
+def run_streamed_suite(args):
+    """Modes A, B and C of sgd_update_k128 (sgd_kernel.cu:125-720) on the c2 ratings held in
+    pinned host memory: updates/s over the training phase (wall clock: the host<->device
+    copies of rating blocks and factor segments are inside it for modes B and C), total wall
+    time and test RMSE after the same number of epochs."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth, build
+    build.build()
+    spec = synth.C2 if args.scale >= 1.0 else synth.scaled(synth.C2, args.scale)
+    train, test = synth.generate(spec, seed=0, device="cuda")
+    m, n, nnz = spec.m, spec.n, len(train)
+    prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=m, n=n, pinned=True)
+    tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"], m=m, n=n)
+    sm, _, _ = cm.device_info(0)
+    epochs = max(1, min(args.steps, 20))
+    for grid in [(1, 1, 1, 1), (2, 2, 1, 1), (4, 1, 1, 1), (1, 1, 2, 2), (2, 2, 2, 2)]:
+        u, v, x, y = grid
+        blocks = u * v * x * y
+        workers = cm.auto_workers(max(1, nnz // blocks), sm, K, "fp16", 0)
+        par = cm.Parameter(k=K, num_workers=workers, num_iters=epochs, lambda_p=0.05, lambda_q=0.05, alpha=0.08,
+                           beta=0.3, seed=0, gpu=0, precision="fp16", u_grid=u, v_grid=v, x_grid=x, y_grid=y, quiet=1)
+        cm.sgd_train(prob, None, cm.Parameter(**{**par.__dict__, "num_iters": 1}))  # warm-up
+        t0 = time.perf_counter()
+        model, st = cm.sgd_train(prob, None, par, with_stats=True)
+        wall = time.perf_counter() - t0
+        rmse = cm.calc_rmse(tprob, model)
+        mode = "A" if blocks == 1 else ("C" if x * y > 1 else "B")
+        print(json.dumps({"suite": "streamed", "mode": mode, "u_v_x_y": grid, "workers_per_block": workers,
+                          "epochs": epochs, "train_ms": st.train_ms, "updates_per_sec": nnz * epochs / (st.train_ms * 1e-3),
+                          "wall_s": wall, "prep_ms": st.prep_ms, "export_ms": st.export_ms,
+                          "test_rmse": rmse}), flush=True)
+        del model
+
+
 def _has_cuda():
     try:
         import torch
@@ -673,7 +708,8 @@ def main():
     ap.add_argument("--warm-configs",
                     default="bf16sr:0.04:0.3:4,bf16sr:0.02:0.05:8,bf16sr:0.04:0.3:2,fp16:0.04:0.3:4,bf16sr:0.02:0.3:0",
                     help="warm-start refinements as storage:alpha:beta:new_user_epochs, comma separated")
-    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm", "text"],
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm", "text",
+                                                    "streamed"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
     if args.suite == "precision":
@@ -690,6 +726,9 @@ def main():
         return
     if args.suite == "text":
         run_text_suite(args)
+        return
+    if args.suite == "streamed":
+        run_streamed_suite(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)
