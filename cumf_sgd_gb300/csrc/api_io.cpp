@@ -485,11 +485,17 @@ int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, i
     if (u_seg_out) *u_seg_out = u_seg;
     if (v_seg_out) *v_seg_out = v_seg;
     const int G = ux * vy;
-    auto gid = [&](const cumf_node &x) -> int64_t { return (x.u / u_seg) * vy + x.v / v_seg; };
+    // Block id (u / u_seg) * vy + v / v_seg in 32-bit unsigned arithmetic (segments fit in
+    // 32 bits; a negative id becomes a large one and is rejected by the range check).
+    const uint32_t us = (uint32_t)u_seg, vs = (uint32_t)v_seg;
+    auto gid = [&](const cumf_node &x) -> int64_t {
+        return (int64_t)((uint32_t)x.u / us) * vy + (int64_t)((uint32_t)x.v / vs);
+    };
     for (int g = 0; g < G; ++g) grid_size[g] = 0;
     for (int64_t i = 0; i < nnz; ++i) {
+        if (R[i].u < 0 || R[i].v < 0) return fail(CUMF_ERR_RANGE, "rating outside the grid");
         const int64_t g = gid(R[i]);
-        if (g < 0 || g >= G) return fail(CUMF_ERR_RANGE, "rating outside the grid");
+        if (g >= G) return fail(CUMF_ERR_RANGE, "rating outside the grid");
         ++grid_size[g];
     }
     // Bucket in place with the reference's cycle swaps (sgd.cu:455-482): the walk of each

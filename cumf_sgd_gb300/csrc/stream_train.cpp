@@ -181,19 +181,34 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     const int k = p.k;
     const int ux = p.ux, vy = p.vy;
 
-    // Working copy of the ratings (the caller's problem is const).
+    // Working copy of the ratings (the caller's problem is const), copied by the host threads.
     PinnedBuf R_pin;
     CUMF_CUDA(cudaMallocHost(&R_pin.p, std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
     cumf_node *R = static_cast<cumf_node *>(R_pin.p);
-    memcpy(R, tr->R, nnz * sizeof(cumf_node));
+    const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(64, nnz / 65536));
+    parallel_for(chunks, [&](int64_t c) {
+        const int64_t a = nnz * c / chunks, b = nnz * (c + 1) / chunks;
+        memcpy(R + a, tr->R + a, (size_t)(b - a) * sizeof(cumf_node));
+    });
 
-    // collect_data (sgd.cu:78-96), serial in fp64 like the reference.
+    // collect_data (sgd.cu:78-96): fp64 sums per chunk, added in chunk order (the float mean
+    // and deviation equal the serial sums' as on the device path of mode A).
     Prepared pr;
+    std::vector<double> p1(chunks, 0.0), p2(chunks, 0.0);
+    parallel_for(chunks, [&](int64_t c) {
+        double a1 = 0, a2 = 0;
+        for (int64_t i = nnz * c / chunks; i < nnz * (c + 1) / chunks; ++i) {
+            const double r = (double)R[i].r;
+            a1 += r;
+            a2 += r * r;
+        }
+        p1[c] = a1;
+        p2[c] = a2;
+    });
     double s1 = 0, s2 = 0;
-    for (int64_t i = 0; i < nnz; ++i) {
-        const double r = (double)R[i].r;
-        s1 += r;
-        s2 += r * r;
+    for (int64_t c = 0; c < chunks; ++c) {
+        s1 += p1[c];
+        s2 += p2[c];
     }
     finish_stats(s1, s2, nnz, pr);
     make_maps((uint32_t)p.seed, m, n, pr);
