@@ -659,7 +659,7 @@ def run_streamed_suite(args):
     tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"], m=m, n=n)
     sm, _, _ = cm.device_info(0)
     epochs = max(1, min(args.steps, 20))
-    for grid in [(1, 1, 1, 1), (2, 2, 1, 1), (4, 1, 1, 1), (1, 1, 2, 2), (2, 2, 2, 2)]:
+    for grid in [(1, 1, 1, 1), (2, 2, 1, 1), (4, 1, 1, 1), (2, 1, 2, 2), (2, 2, 2, 2)]:
         u, v, x, y = grid
         blocks = u * v * x * y
         workers = cm.auto_workers(max(1, nnz // blocks), sm, K, "fp16", 0)
@@ -670,7 +670,7 @@ def run_streamed_suite(args):
         model, st = cm.sgd_train(prob, None, par, with_stats=True)
         wall = time.perf_counter() - t0
         rmse = cm.calc_rmse(tprob, model)
-        mode = "A" if blocks == 1 else ("C" if x * y > 1 else "B")
+        mode = "ABC"[st.mode]
         print(json.dumps({"suite": "streamed", "mode": mode, "u_v_x_y": grid, "workers_per_block": workers,
                           "epochs": epochs, "train_ms": st.train_ms, "updates_per_sec": nnz * epochs / (st.train_ms * 1e-3),
                           "wall_s": wall, "prep_ms": st.prep_ms, "export_ms": st.export_ms,

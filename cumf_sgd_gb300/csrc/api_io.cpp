@@ -9,6 +9,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <memory>
 #include <cctype>
 #include <cmath>
 #include <string>
@@ -56,6 +57,36 @@ static void host_free(void *p, int pinned) {
         cudaFreeHost(p);
     else
         free(p);
+}
+
+// Block g's walk (sgd.cu:466-481): its slots from the first one not yet filled by earlier
+// blocks' swaps; the record held at the walk position either belongs to g (it stays, the walk
+// advances) or goes to the next free slot of its own block, whose original record is taken
+// in its place.  Slots at or past a block's free pointer still hold their original records,
+// so only the original block ids are read.
+void grid_order(const int32_t *bid, int64_t nnz, int G, const int64_t *grid_size, int64_t *fin) {
+    std::vector<int64_t> begin(G + 1, 0), free_slot(G);
+    for (int g = 0; g < G; ++g) begin[g + 1] = begin[g] + grid_size[g];
+    for (int g = 0; g < G; ++g) free_slot[g] = begin[g];
+    if (nnz <= 0) return;
+    for (int g = 0; g < G; ++g) {
+        int64_t p = free_slot[g];
+        const int64_t end = begin[g + 1];
+        if (p >= end) continue;
+        int64_t cur = p;  // original index of the record held at the walk position
+        while (true) {
+            const int c = bid[cur];
+            if (c == g) {
+                fin[p] = cur;
+                if (++p >= end) break;
+                cur = p;
+            } else {
+                const int64_t slot = free_slot[c]++;
+                fin[slot] = cur;
+                cur = slot;
+            }
+        }
+    }
 }
 
 }  // namespace cumf
@@ -485,36 +516,43 @@ int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, i
     if (u_seg_out) *u_seg_out = u_seg;
     if (v_seg_out) *v_seg_out = v_seg;
     const int G = ux * vy;
-    // Block id (u / u_seg) * vy + v / v_seg in 32-bit unsigned arithmetic (segments fit in
-    // 32 bits; a negative id becomes a large one and is rejected by the range check).
-    const uint32_t us = (uint32_t)u_seg, vs = (uint32_t)v_seg;
-    auto gid = [&](const cumf_node &x) -> int64_t {
-        return (int64_t)((uint32_t)x.u / us) * vy + (int64_t)((uint32_t)x.v / vs);
-    };
-    for (int g = 0; g < G; ++g) grid_size[g] = 0;
-    for (int64_t i = 0; i < nnz; ++i) {
-        if (R[i].u < 0 || R[i].v < 0) return fail(CUMF_ERR_RANGE, "rating outside the grid");
-        const int64_t g = gid(R[i]);
-        if (g >= G) return fail(CUMF_ERR_RANGE, "rating outside the grid");
-        ++grid_size[g];
-    }
-    // Bucket in place with the reference's cycle swaps (sgd.cu:455-482): the walk of each
-    // block pushes foreign records to the next free slot of their own block.  The order is
-    // a sequential function of the input, so this pass stays on the host.
-    std::vector<int64_t> begin(G + 1, 0), pivot(G);
-    for (int g = 0; g < G; ++g) begin[g + 1] = begin[g] + grid_size[g];
-    for (int g = 0; g < G; ++g) pivot[g] = begin[g];
-    for (int g = 0; g < G; ++g) {
-        for (int64_t p = pivot[g]; p != begin[g + 1];) {
-            const int64_t c = gid(R[p]);
-            if (c == g) {
-                ++p;
+    // Block ids (u / u_seg) * vy + v / v_seg in 32-bit unsigned arithmetic, and the counts.
+    const uint32_t us = (uint32_t)std::max<int64_t>(1, u_seg), vs = (uint32_t)std::max<int64_t>(1, v_seg);
+    std::unique_ptr<int32_t[]> bid(new int32_t[(size_t)std::max<int64_t>(1, nnz)]);  // filled by the threads
+    std::vector<std::vector<int64_t>> part(16, std::vector<int64_t>(G, 0));
+    std::vector<int> bad(16, 0);
+    parallel_chunks(nnz, [&](int64_t a, int64_t b, int t) {
+        for (int64_t i = a; i < b; ++i) {
+            const cumf_node x = R[i];
+            const int64_t g = (x.u < 0 || x.v < 0) ? G : (int64_t)((uint32_t)x.u / us) * vy + (int64_t)((uint32_t)x.v / vs);
+            if (g >= G) {
+                bad[t] = 1;
+                bid[i] = 0;
                 continue;
             }
-            std::swap(R[p], R[pivot[c]]);
-            ++pivot[c];
+            bid[i] = (int32_t)g;
+            ++part[t][g];
         }
+    });
+    for (int t = 0; t < 16; ++t)
+        if (bad[t]) return fail(CUMF_ERR_RANGE, "rating outside the grid");
+    for (int g = 0; g < G; ++g) {
+        grid_size[g] = 0;
+        for (int t = 0; t < 16; ++t) grid_size[g] += part[t][g];
     }
+    // The reference's cycle-swap order, replayed on the ids, then one gather of the records.
+    std::unique_ptr<int64_t[]> fin(new int64_t[(size_t)std::max<int64_t>(1, nnz)]);
+    parallel_chunks(nnz, [&](int64_t a, int64_t b, int) {  // map the pages on all threads first
+        if (b > a) memset(fin.get() + a, 0, (size_t)(b - a) * sizeof(int64_t));
+    });
+    grid_order(bid.get(), nnz, G, grid_size, fin.get());
+    std::unique_ptr<cumf_node[]> tmp(new cumf_node[(size_t)std::max<int64_t>(1, nnz)]);
+    parallel_chunks(nnz, [&](int64_t a, int64_t b, int) {
+        for (int64_t i = a; i < b; ++i) tmp[i] = R[fin[i]];
+    });
+    parallel_chunks(nnz, [&](int64_t a, int64_t b, int) {
+        if (b > a) memcpy(R + a, tmp.get() + a, (size_t)(b - a) * sizeof(cumf_node));
+    });
     return CUMF_OK;
 }
 

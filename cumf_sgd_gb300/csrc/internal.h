@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "cumf_sgd.h"
 
@@ -76,6 +79,22 @@ cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, 
 
 // Order-independent digest of `bytes` (a multiple of 4) at d into *d_out.
 cudaError_t launch_digest(const void *d, uint64_t bytes, unsigned long long *d_out, cudaStream_t s);
+
+// f(a, b, t) over [0, n) split into contiguous chunks, one per host thread (at most 16).
+template <typename F>
+void parallel_chunks(int64_t n, F f) {
+    const int64_t T = std::max<int64_t>(1, std::min<int64_t>(std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency())),
+                                                             n / 65536 + 1));
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < T; ++t) th.emplace_back([&, t] { f(n * t / T, n * (t + 1) / T, (int)t); });
+    for (auto &x : th) x.join();
+}
+
+// grid_problem's in-place bucketing (sgd.cu:455-482) replayed on block ids: fin[slot] = the
+// original index of the record that the reference's cycle swaps leave in that slot.  bid[i]
+// is record i's block (0 <= bid < G); grid_size holds the counts.  Same order as swapping the
+// records, without moving them: each step reads one block id and writes one index.
+void grid_order(const int32_t *bid, int64_t nnz, int G, const int64_t *grid_size, int64_t *fin);
 
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -181,51 +182,73 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     const int k = p.k;
     const int ux = p.ux, vy = p.vy;
 
-    // Working copy of the ratings (the caller's problem is const), copied by the host threads.
+    // Preparation on the host threads, equal to the reference's sequence collect_data,
+    // shuffle_problem, grid_problem, scale_problem (sgd.cu:648-674) on a working copy:
+    //   pass 1: rating sums (fp64 per chunk, added in chunk order) and the block id of every
+    //           shuffled record, with per-block counts;
+    //   grid_order: grid_problem's swap order replayed on the block ids;
+    //   pass 2: the working copy gathered in that order from the caller's records, shuffled
+    //           and scaled with block-local ids in the same step.
+    Prepared pr;
+    make_maps((uint32_t)p.seed, m, n, pr);
+    const int32_t *pm = pr.pmap.data(), *qm = pr.qmap.data();
+    const int64_t u_seg = ux == 1 ? m : (int64_t)ceil((double)m / ux);  // sgd.cu:419-426
+    const int64_t v_seg = vy == 1 ? n : (int64_t)ceil((double)n / vy);
+    const uint32_t us = (uint32_t)std::max<int64_t>(1, u_seg), vs = (uint32_t)std::max<int64_t>(1, v_seg);
+    const int G = ux * vy;
+    std::unique_ptr<int32_t[]> bid(new int32_t[(size_t)std::max<int64_t>(1, nnz)]);  // filled by the threads
+    std::vector<double> p1(16, 0.0), p2(16, 0.0);
+    std::vector<std::vector<int64_t>> part(16, std::vector<int64_t>(G, 0));
+    std::vector<int> bad(16, 0);
+    parallel_chunks(nnz, [&](int64_t a0, int64_t b0, int t) {
+        double a1 = 0, a2 = 0;
+        for (int64_t i = a0; i < b0; ++i) {
+            const cumf_node x = tr->R[i];
+            const double r = (double)x.r;
+            a1 += r;
+            a2 += r * r;
+            if (x.u < 0 || x.u >= m || x.v < 0 || x.v >= n) {
+                bad[t] = 1;
+                bid[i] = 0;
+                continue;
+            }
+            const int32_t g = (int32_t)(((uint32_t)pm[x.u] / us) * (uint32_t)vy + (uint32_t)qm[x.v] / vs);
+            bid[i] = g;
+            ++part[t][g];
+        }
+        p1[t] = a1;
+        p2[t] = a2;
+    });
+    for (int t = 0; t < 16; ++t)
+        if (bad[t]) return fail(CUMF_ERR_RANGE, "rating outside the grid");
+    double s1 = 0, s2 = 0;
+    for (int t = 0; t < 16; ++t) {
+        s1 += p1[t];
+        s2 += p2[t];
+    }
+    finish_stats(s1, s2, nnz, pr);
+    std::vector<int64_t> grid_size(G, 0);
+    for (int g = 0; g < G; ++g)
+        for (int t = 0; t < 16; ++t) grid_size[g] += part[t][g];
+    std::unique_ptr<int64_t[]> fin(new int64_t[(size_t)std::max<int64_t>(1, nnz)]);
+    parallel_chunks(nnz, [&](int64_t a, int64_t b, int) {  // map the pages on all threads first
+        if (b > a) memset(fin.get() + a, 0, (size_t)(b - a) * sizeof(int64_t));
+    });
+    grid_order(bid.get(), nnz, G, grid_size.data(), fin.get());
+    bid.reset();
     PinnedBuf R_pin;
     CUMF_CUDA(cudaMallocHost(&R_pin.p, std::max<int64_t>(1, nnz) * sizeof(cumf_node)));
     cumf_node *R = static_cast<cumf_node *>(R_pin.p);
-    const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(64, nnz / 65536));
-    parallel_for(chunks, [&](int64_t c) {
-        const int64_t a = nnz * c / chunks, b = nnz * (c + 1) / chunks;
-        memcpy(R + a, tr->R + a, (size_t)(b - a) * sizeof(cumf_node));
-    });
-
-    // collect_data (sgd.cu:78-96): fp64 sums per chunk, added in chunk order (the float mean
-    // and deviation equal the serial sums' as on the device path of mode A).
-    Prepared pr;
-    std::vector<double> p1(chunks, 0.0), p2(chunks, 0.0);
-    parallel_for(chunks, [&](int64_t c) {
-        double a1 = 0, a2 = 0;
-        for (int64_t i = nnz * c / chunks; i < nnz * (c + 1) / chunks; ++i) {
-            const double r = (double)R[i].r;
-            a1 += r;
-            a2 += r * r;
-        }
-        p1[c] = a1;
-        p2[c] = a2;
-    });
-    double s1 = 0, s2 = 0;
-    for (int64_t c = 0; c < chunks; ++c) {
-        s1 += p1[c];
-        s2 += p2[c];
-    }
-    finish_stats(s1, s2, nnz, pr);
-    make_maps((uint32_t)p.seed, m, n, pr);
-    const int32_t *pm = pr.pmap.data(), *qm = pr.qmap.data();
-    parallel_for(nnz, [&](int64_t i) {  // shuffle_problem (sgd.cu:126-134)
-        R[i].u = pm[R[i].u];
-        R[i].v = qm[R[i].v];
-    });
-    std::vector<int64_t> grid_size(ux * vy);
-    int64_t u_seg = 0, v_seg = 0;
-    if (int rc = cumf_grid_problem(R, nnz, m, n, ux, vy, grid_size.data(), &u_seg, &v_seg)) return rc;
     const float rscale = (float)(1.0 / pr.scale);
-    parallel_for(nnz, [&](int64_t i) {  // scale_problem (sgd.cu:98-124)
-        R[i].r = R[i].r * rscale;
-        R[i].u = (int32_t)(R[i].u % u_seg);
-        R[i].v = (int32_t)(R[i].v % v_seg);
+    parallel_chunks(nnz, [&](int64_t a0, int64_t b0, int) {
+        for (int64_t i = a0; i < b0; ++i) {
+            const cumf_node x = tr->R[fin[i]];
+            R[i].u = (int32_t)(pm[x.u] % u_seg);
+            R[i].v = (int32_t)(qm[x.v] % v_seg);
+            R[i].r = x.r * rscale;
+        }
     });
+    fin.reset();
     const float lambda_p = p.lambda_p / pr.scale, lambda_q = p.lambda_q / pr.scale;
     std::vector<int64_t> begin(ux * vy + 1, 0);
     for (int g = 0; g < ux * vy; ++g) begin[g + 1] = begin[g] + grid_size[g];
