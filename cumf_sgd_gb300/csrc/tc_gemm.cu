@@ -334,6 +334,200 @@ tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_const
     }
 }
 
+// ---- persistent variant (many output tiles, no split K) ----------------------------------
+//
+// One CTA per SM walks tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... (the two n-tiles of an
+// m-block are adjacent, so their A rows are read once from DRAM).  Warp 0 (one lane) streams
+// operand stages through the ring across tile boundaries; warp 1 (one lane) issues the MMAs
+// into one of two tensor-memory accumulators (tile j uses accumulator j % 2) and commits
+// `tfull`; warps 2-5 drain an accumulator (tcgen05.ld, bias, activation, staged coalesced
+// stores) and release it through `tempty` while the next tile's MMAs fill the other one.
+constexpr int kPersThreads = 192;
+
+template <int BN, int kStages>
+struct PersSmem {
+    static constexpr int A_BYTES = kTcBM * 128;
+    static constexpr int B_BYTES = BN * 128;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int STG = 4 * 32 * kStgStride * 4;  // four epilogue warps' staging blocks
+    static constexpr int TOTAL = 1024 + kStages * STAGE + STG + 256;
+};
+
+__device__ __forceinline__ bool aborted(const int *flag) { return *reinterpret_cast<const volatile int *>(flag) != 0; }
+
+template <int BN, int kStages>
+__global__ void __launch_bounds__(kPersThreads, 1)
+tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
+                          int N, int K, const float *__restrict__ bias, int act, void *out, int out_f32, int ldo,
+                          float *pre_out, int *status) {
+    using S = PersSmem<BN, kStages>;
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;  // swizzle atoms need 1024-byte alignment
+    unsigned char *aligned = smem_raw + (base - raw);
+    float *stg_all = reinterpret_cast<float *>(aligned + kStages * S::STAGE);
+    uint64_t *full = reinterpret_cast<uint64_t *>(aligned + kStages * S::STAGE + S::STG);
+    uint64_t *empty = full + kStages;
+    uint64_t *tfull = empty + kStages;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *mma_done = tempty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+    int *issued_slot = abort_flag + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_n = (N + BN - 1) / BN;
+    const int tiles = ((M + kTcBM - 1) / kTcBM) * tiles_n;
+    const int my_tiles = (int)blockIdx.x < tiles ? (tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const int KT = (K + kTcBK - 1) / kTcBK;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[i])));
+        }
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&tfull[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(&tempty[i])));  // one per epilogue warp
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mma_done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        *abort_flag = 0;
+        *issued_slot = 0;
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(2 * BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // TMA producer
+            int it = 0;
+            for (int j = 0; j < my_tiles && !aborted(abort_flag); ++j) {
+                const int t = (int)blockIdx.x + j * (int)gridDim.x;
+                const int tm = t / tiles_n, tn = t % tiles_n;
+                for (int kk = 0; kk < KT; ++kk, ++it) {
+                    const int st = it % kStages;
+                    if (it >= kStages && !mbar_wait(smem_u32(&empty[st]), ((it / kStages) - 1) & 1)) {
+                        atomicExch(abort_flag, 1);
+                        break;
+                    }
+                    const uint32_t fb = smem_u32(&full[st]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(S::STAGE)
+                                 : "memory");
+                    const uint32_t a_dst = base + st * S::STAGE;
+                    tma_load_2d(a_dst, &map_a, kk * kTcBK, tm * kTcBM, fb);
+                    tma_load_2d(a_dst + S::A_BYTES, &map_b, kk * kTcBK, tn * BN, fb);
+                    *issued_slot = it + 1;
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            int it = 0;
+            bool ok = true;
+            for (int j = 0; j < my_tiles && ok; ++j) {
+                const int acc = j & 1;
+                if (j >= 2 && !mbar_wait(smem_u32(&tempty[acc]), ((j >> 1) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(acc * BN);
+                for (int kk = 0; kk < KT; ++kk, ++it) {
+                    const int st = it % kStages;
+                    if (!mbar_wait(smem_u32(&full[st]), (it / kStages) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t a0 = base + st * S::STAGE, b0 = a0 + S::A_BYTES;
+#pragma unroll
+                    for (int sub = 0; sub < kTcBK / 16; ++sub) {
+                        const uint32_t accum = (kk > 0 || sub > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                            "l"(sw128_desc(a0 + sub * 32)), "l"(sw128_desc(b0 + sub * 32)), "r"(instr_desc<BN>()),
+                            "r"(accum));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     smem_u32(&empty[st]))
+                                 : "memory");
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smem_u32(&tfull[acc]))
+                             : "memory");
+            }
+            if (!ok) atomicExch(abort_flag, 1);
+            // Tracks every MMA issued above: the accumulators may be freed once it completes.
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(mma_done))
+                         : "memory");
+        }
+    } else {  // epilogue warps 2-5: tensor-memory lanes 32 (warp % 4)..
+        const int quarter = warp & 3;
+        float *stg = stg_all + (warp - 2) * (32 * kStgStride);
+        for (int j = 0; j < my_tiles; ++j) {
+            const int acc = j & 1;
+            const int t = (int)blockIdx.x + j * (int)gridDim.x;
+            const int tm = t / tiles_n, tn = t % tiles_n;
+            int ok = mbar_wait(smem_u32(&tfull[acc]), (j >> 1) & 1) ? 1 : 0;
+            ok = __all_sync(0xffffffffu, ok) && !aborted(abort_flag);
+            if (!ok) {
+                if (lane == 0) atomicExch(abort_flag, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int r0 = tm * kTcBM + quarter * 32, n0 = tn * BN;
+            for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 32) {
+                uint32_t r[32];
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * BN + c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                    "[%32];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                      "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                      "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                epilogue_chunk(stg, r, r0, n0 + c0, M, N, bias, act, out, out_f32, ldo, pre_out, false, lane);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&tempty[acc])) : "memory");
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // Bounded drain: every MMA, then (after an abort) the last copy issued into each stage.
+        mbar_wait(smem_u32(mma_done), 0);
+        if (aborted(abort_flag)) {
+            if (status) atomicExch(status, (int)CUMF_ERR_TIMEOUT);
+            const int issued = *issued_slot;
+            for (int st = 0; st < kStages && st < issued; ++st) {
+                const int last = st + ((issued - 1 - st) / kStages) * kStages;
+                mbar_wait(smem_u32(&full[st]), (last / kStages) & 1);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * BN));
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -381,6 +575,28 @@ cudaError_t launch_variant(dim3 grid, const CUtensorMap &ma, const CUtensorMap &
     return cudaGetLastError();
 }
 
+template <int BN, int ST>
+cudaError_t launch_persistent(int grid, const CUtensorMap &ma, const CUtensorMap &mb, int M, int N, int K,
+                              const float *bias, int act, void *out, int out_f32, int ldo, float *pre_out, int *status,
+                              cudaStream_t s) {
+    const int sm = PersSmem<BN, ST>::TOTAL;
+    cudaError_t e =
+        cudaFuncSetAttribute(tc_gemm_persistent_kernel<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess) return e;
+    tc_gemm_persistent_kernel<BN, ST><<<grid, kPersThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo,
+                                                                     pre_out, status);
+    return cudaGetLastError();
+}
+
+int sm_count_of_current_device() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms;
+}
+
 cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, const float *bias, int act,
                            void *out, int out_f32, int ldo, float *pre_out, int *status, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0 || (K % 8) != 0) return cudaErrorInvalidValue;
@@ -404,6 +620,14 @@ cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, co
             cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
             if (e != cudaSuccess) return e;
         }
+    }
+    // Enough output tiles for two per SM: the persistent kernel, whose epilogues overlap the
+    // next tiles' loads and MMAs.
+    const int sms = sm_count_of_current_device();
+    if (splits == 1 && sms > 0 && (long long)tiles_m * tiles_n >= 2ll * sms) {
+        const int g = std::min(tiles_m * tiles_n, sms);
+        return wide ? launch_persistent<256, 4>(g, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status, s)
+                    : launch_persistent<128, 6>(g, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status, s);
     }
     const dim3 grid(tiles_m, tiles_n, splits);
     if (wide)

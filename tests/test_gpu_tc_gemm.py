@@ -20,7 +20,9 @@ def ref(A, B, bias, act):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 512, 192), (300, 144, 128), (1000, 128, 512),
-                                   (77, 256, 64), (130, 520, 64), (200, 136, 136), (129, 264, 40)])
+                                   (77, 256, 64), (130, 520, 64), (200, 136, 136), (129, 264, 40),
+                                   # persistent kernel (at least two tiles per SM): tails in M, N, K
+                                   (40037, 512, 192), (39001, 128, 520), (20000, 260, 64), (65536, 512, 512)])
 @pytest.mark.parametrize("act", [0, 1])
 def test_tc_gemm_matches_torch_fp32(lib, cuda, M, N, K, act):
     import torch
