@@ -316,7 +316,7 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     int64_t step = 0;
     for (int it = 0; it < p.num_iters; ++it) {
         for (const Step &sp : sched[it]) {
-            int jr, jp, jq;
+            int jr = 0, jp = 0, jq = 0;
             if (int rc = Rc.acquire(sp.g, step, copy.s, r_host, &jr)) return rc;
             if (int rc = Pc.acquire(sp.gx, step, copy.s, p_host, &jp)) return rc;
             if (int rc = Qc.acquire(sp.gy, step, copy.s, q_host, &jq)) return rc;
