@@ -482,6 +482,16 @@ int cumf_auto_workers(int64_t nnz, int sm_count, int k, int precision, int lanes
     return (int)w;
 }
 
+// num_workers 0: cumf_auto_workers for the ratings of one grid block (the whole problem in
+// mode A).
+static int resolve_workers(const cumf_problem *tr, const cumf_params &p, int lanes) {
+    if (p.num_workers > 0) return p.num_workers;
+    int sms = 0;
+    if (cumf_device_info(p.gpu, &sms, nullptr, nullptr) != CUMF_OK || sms <= 0) sms = 148;
+    const int64_t blocks = (int64_t)std::max(1, p.ux) * std::max(1, p.vy);
+    return cumf_auto_workers(std::max<int64_t>(1, tr->nnz / blocks), sms, p.k, p.precision, lanes);
+}
+
 int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params *params,
                cumf_model *out, cumf_train_stats *stats) {
     if (!tr || !out) return fail(CUMF_ERR_ARG, "train: problem and model must not be NULL");
@@ -496,6 +506,7 @@ int cumf_train(const cumf_problem *tr, const cumf_problem *va, const cumf_params
     p.vy = p.v_grid * p.y_grid;
     if (int rc = select_device(p.gpu)) return rc;
     const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    p.num_workers = resolve_workers(tr, p, lanes);
     const int workers = p.num_workers;
     if (!p.quiet) {
         print_args(p);
@@ -522,6 +533,7 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
         return fail(CUMF_ERR_ARG, "train_ex: init model does not match k");
     if (int rc = select_device(p.gpu)) return rc;
     const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    p.num_workers = resolve_workers(tr, p, lanes);
     if (!p.quiet) print_args(p);
     return train_mode_a(tr, te, p, p.num_workers, lanes, out, stats, init, epoch_rmse, epoch_ms);
 }
@@ -543,6 +555,7 @@ int cumf_train_ckpt(const cumf_problem *tr, const cumf_problem *te, const cumf_p
     p.ux = p.vy = 1;
     if (int rc = select_device(p.gpu)) return rc;
     const int lanes = p.lanes ? p.lanes : default_lanes(p.k, p.precision);
+    p.num_workers = resolve_workers(tr, p, lanes);
     if (!p.quiet) print_args(p);
     return train_mode_a(tr, te, p, p.num_workers, lanes, out, stats, nullptr, nullptr, nullptr, ckpt, epochs_done);
 }

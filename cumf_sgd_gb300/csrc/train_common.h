@@ -59,7 +59,7 @@ inline bool valid_k(int k) { return k == 32 || k == 64 || k == 128 || k == 256; 
 inline int check_params(const cumf_params *p) {
     if (!p) return fail(CUMF_ERR_ARG, "params is NULL");
     if (!valid_k(p->k)) return fail(CUMF_ERR_ARG, "k must be 32, 64, 128 or 256 (got " + std::to_string(p->k) + ")");
-    if (p->num_workers < 1) return fail(CUMF_ERR_ARG, "num_workers must be positive");
+    if (p->num_workers < 0) return fail(CUMF_ERR_ARG, "num_workers must be >= 0 (0 = automatic)");
     if (p->num_iters < 0) return fail(CUMF_ERR_ARG, "num_iters must be >= 0");
     if (p->u_grid < 1 || p->v_grid < 1 || p->x_grid < 1 || p->y_grid < 1)
         return fail(CUMF_ERR_ARG, "grid sizes must be positive");

@@ -83,7 +83,8 @@ typedef struct cumf_problem {
  * fills the reference defaults (sgd.h:45). */
 typedef struct cumf_params {
     int32_t k;             /* factor length; 32, 64, 128 or 256 (reference: 128 only)  */
-    int32_t num_workers;   /* -s: Hogwild workers; rounded up to a multiple of 4         */
+    int32_t num_workers;   /* -s: Hogwild workers; rounded up to a multiple of 4; 0 = automatic
+                              (cumf_auto_workers for the ratings of one grid block)         */
     int32_t u_grid, v_grid, x_grid, y_grid;   /* -u -v -x -y                            */
     int32_t ux, vy;        /* u_grid*x_grid, v_grid*y_grid (main.cpp:224-225)           */
     int32_t num_iters;     /* -t                                                        */

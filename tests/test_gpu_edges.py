@@ -90,3 +90,16 @@ def test_empty_problem_trains(lib, cuda, grid):
     assert model.P.shape == (7, 32) and model.Q.shape == (5, 32)
     assert np.isfinite(model.P).all() and np.isfinite(model.Q).all()
     assert model.b == 0.0
+
+
+def test_zero_workers_means_automatic(lib, cuda):
+    rng = np.random.default_rng(3)
+    nnz, m, n = 200_000, 2000, 500
+    prob = cm.MFProblem.from_arrays(rng.integers(0, m, nnz), rng.integers(0, n, nnz),
+                                    rng.integers(1, 6, nnz).astype(np.float32), m=m, n=n)
+    sm, _, _ = cm.device_info(0)
+    for grid in ((1, 1), (2, 2)):
+        par = cm.Parameter(k=64, num_workers=0, num_iters=2, u_grid=grid[0], v_grid=grid[1], seed=1, gpu=0, quiet=1)
+        _, st = cm.sgd_train(prob, None, par, with_stats=True)
+        blocks = grid[0] * grid[1]
+        assert st.num_workers == cm.auto_workers(nnz // blocks, sm, 64, "fp16", 0)

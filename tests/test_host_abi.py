@@ -168,7 +168,7 @@ def test_lr_schedule_and_budget(lib, orc):
 
 def test_train_rejects_bad_parameters_without_gpu(lib):
     prob = cm.MFProblem.from_arrays([0, 1], [0, 1], [1.0, 2.0])
-    for kw in (dict(k=100), dict(k=128, num_workers=0), dict(k=128, lanes=3), dict(k=128, num_iters=-1)):
+    for kw in (dict(k=100), dict(k=128, num_workers=-1), dict(k=128, lanes=3), dict(k=128, num_iters=-1)):
         with pytest.raises(cm.CumfError) as e:
             cm.sgd_train(prob, None, cm.Parameter(**kw))
         assert e.value.code == _lib.CUMF_ERR_ARG
