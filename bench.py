@@ -45,6 +45,33 @@ def dist_env():
     return rank, world, local
 
 
+def init_dist(world: int) -> None:
+    """One process per GPU under torchrun: NCCL with CUDA, gloo without (CPU tests)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest value over all ranks (the slowest replica's time), returned on every rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -164,7 +191,7 @@ def run_reference_arm(args):
             per_step.append(base)
     v = statistics.mean(b["value"] for b in per_step)
     line = {"impl": "reference", "metric": "sgd_updates_per_sec", "value": v, "unit": "updates/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "storage": "fp32 (CPU port)", "k": K},
             "cpu_baseline": dict(per_step[-1], value=v),
@@ -740,9 +767,7 @@ def main():
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    init_dist(world)
     build.build()
     spec = synth.C2 if args.scale >= 1.0 else synth.scaled(synth.C2, args.scale)
     train, test = synth.generate(spec, seed=rank, device="cuda")
@@ -785,8 +810,7 @@ def main():
     for e in range(args.warmup):
         epoch(e)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -798,11 +822,8 @@ def main():
     ms = ev0.elapsed_time(ev1)
     clocks = clk.summary()
     assert int(status.item()) == 0, "update kernel flagged an out-of-range index"
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+    ms = max_over_ranks(ms, world)
+    barrier(world)
     secs = ms / 1e3
     updates_per_sec = nnz * args.steps * world / secs
     batches = cm.batches_per_worker(nnz, workers)
@@ -823,9 +844,10 @@ def main():
         par = cm.Parameter(k=K, num_workers=workers, num_iters=args.e2e_epochs, lambda_p=0.05, lambda_q=0.05,
                            alpha=0.08, beta=0.3, seed=rank, gpu=local, precision=prec, lanes=args.lanes)
         cm.sgd_train(prob, None, cm.Parameter(**{**par.__dict__, "num_iters": 1}))  # warm-up call
+        barrier(world)
         t0 = time.perf_counter()
         model, st = cm.sgd_train(prob, None, par, with_stats=True)
-        wall = time.perf_counter() - t0
+        wall = max_over_ranks(time.perf_counter() - t0, world)  # the slowest replica
         test_rmse = cm.calc_rmse(tprob, model)
         e2e = {"value": nnz * args.e2e_epochs * world / wall, "unit": "updates/s",
                "h2d_bytes_per_step": nnz * 12 + 4 * (m + n), "d2h_bytes_per_step": 4 * K * (m + n),
