@@ -101,6 +101,7 @@ _SIGS = {
     "cumf_write_problem": (C.c_int, [C.c_char_p, C.POINTER(Problem)]),
     "cumf_train_ckpt": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Checkpoint),
                                   C.POINTER(Model), C.POINTER(TrainStats), C.POINTER(C.c_int32)]),
+    "cumf_selftest_wait_timeout": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),

@@ -30,6 +30,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "cumf_sgd.h"
 #include "internal.h"
@@ -42,7 +43,8 @@ constexpr int kTcThreads = 256;  // 8 warps: all read the accumulator in the epi
 constexpr int kStgStride = 36;    // floats per staged row (144 bytes: 16-byte aligned, conflict-free)
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;
-constexpr long long kSpinLimit = 1ll << 24;  // try_wait polls before giving up (seconds)
+constexpr unsigned long long kWaitNs = 2000000000ull;  // an mbarrier wait gives up after 2 s
+constexpr long long kSpinLimit = 1ll << 28;            // and after this many polls in any case
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -55,7 +57,15 @@ __device__ __forceinline__ uint32_t instr_desc() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the phase of parity `parity` of an mbarrier; false after kWaitNs of global time.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    const unsigned long long t0 = global_ns();
     for (long long i = 0; i < kSpinLimit; ++i) {
         uint32_t done;
         asm volatile(
@@ -64,6 +74,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
             : "r"(mbar), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((i & 63) == 63 && global_ns() - t0 > kWaitNs) return false;
     }
     return false;
 }
@@ -206,7 +217,7 @@ template <int BN, int kStages>
 __global__ void __launch_bounds__(kTcThreads, kStages == 2 ? 2 : 1)
 tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
                    int N, int K, const float *__restrict__ bias, int act, void *out, int out_f32, int ldo,
-                   float *pre_out, int *status, int splits) {
+                   float *pre_out, int *status, int splits, int no_copies) {
     using S = TmaSmem<BN, kStages>;
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
@@ -247,7 +258,7 @@ tc_gemm_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_const
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (threadIdx.x == 0 && KT > 0) {  // TMA producer
+    if (threadIdx.x == 0 && KT > 0 && !no_copies) {  // TMA producer (no_copies: the wait self-test)
         for (int i = 0; i < KT; ++i) {
             const int st = i % kStages;
             if (i >= kStages && !mbar_wait(smem_u32(&empty[st]), ((i / kStages) - 1) & 1)) {
@@ -566,12 +577,12 @@ bool make_map(CUtensorMap *map, const void *ptr, int rows, int K, int box_rows) 
 template <int BN, int ST>
 cudaError_t launch_variant(dim3 grid, const CUtensorMap &ma, const CUtensorMap &mb, int M, int N, int K,
                            const float *bias, int act, void *out, int out_f32, int ldo, float *pre_out, int *status,
-                           int splits, cudaStream_t s) {
+                           int splits, cudaStream_t s, int no_copies = 0) {
     const int sm = TmaSmem<BN, ST>::TOTAL;
     cudaError_t e = cudaFuncSetAttribute(tc_gemm_tma_kernel<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e != cudaSuccess) return e;
     tc_gemm_tma_kernel<BN, ST><<<grid, kTcThreads, sm, s>>>(ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out,
-                                                            status, splits);
+                                                            status, splits, no_copies);
     return cudaGetLastError();
 }
 
@@ -653,4 +664,67 @@ extern "C" int cumf_tc_gemm(const void *d_A, const void *d_B, int M, int N, int 
     CUMF_CUDA(launch_tc_gemm(d_A, d_B, M, N, K, d_bias, act, d_out, out_f32, ldo, d_pre, d_status,
                              (cudaStream_t)stream));
     return CUMF_OK;
+}
+
+extern "C" int cumf_selftest_wait_timeout(int *status_out, double *seconds) {
+    if (!status_out) return fail(CUMF_ERR_ARG, "selftest: status_out is NULL");
+    *status_out = 0;
+    // One 128 x 128 x 64 tile whose producer issues no copies: the MMA thread's wait on the
+    // stage barrier runs out, the kernel records CUMF_ERR_TIMEOUT, drains and frees its tensor
+    // memory; then an ordinary product on the same context must still be right.
+    const int M = 128, N = 128, K = 64;
+    void *buf = nullptr;
+    const size_t ab = (size_t)M * K * 2, bb = (size_t)N * K * 2, ob = (size_t)M * N * 4;
+    CUMF_CUDA(cudaMalloc(&buf, ab + bb + ob + 16));
+    char *A = static_cast<char *>(buf);
+    char *B = A + ab;
+    float *O = reinterpret_cast<float *>(B + bb);
+    int *st = reinterpret_cast<int *>(reinterpret_cast<char *>(O) + ob);
+    int rc = CUMF_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    do {
+        cudaError_t e = cudaMemset(buf, 0, ab + bb + ob + 16);
+        if (e == cudaSuccess) {  // A = B = bf16 1.0: every output element is K
+            std::vector<uint16_t> ones((M > N ? M : N) * K, 0x3f80);
+            e = cudaMemcpy(A, ones.data(), ab, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(B, ones.data(), bb, cudaMemcpyHostToDevice);
+        }
+        CUtensorMap ma, mb;
+        if (e == cudaSuccess && (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, 128))) {
+            rc = fail(CUMF_ERR_CUDA, "selftest: tensor maps");
+            break;
+        }
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+        if (e == cudaSuccess)
+            e = launch_variant<128, 2>(dim3(1, 1, 1), ma, mb, M, N, K, nullptr, 0, O, 1, N, nullptr, st, 1, 0, 1);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess) e = cudaMemcpy(status_out, st, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "selftest: timed-out launch");
+            break;
+        }
+        if (seconds) *seconds = ms * 1e-3;
+        // The context is usable: an ordinary product gives K everywhere.
+        e = launch_tc_gemm(A, B, M, N, K, nullptr, 0, O, 1, N, nullptr, nullptr, 0);
+        std::vector<float> host((size_t)M * N, 0.f);
+        if (e == cudaSuccess) e = cudaMemcpy(host.data(), O, ob, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "selftest: product after the timeout");
+            break;
+        }
+        for (float v : host)
+            if (v != (float)K) {
+                rc = fail(CUMF_ERR_CUDA, "selftest: product after the timeout is wrong");
+                break;
+            }
+    } while (0);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(buf);
+    return rc;
 }

@@ -376,6 +376,13 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
                   const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
                   double *epoch_ms);
 
+/* Self-test of the bounded waits (no reference counterpart): one tensor-core product whose
+ * operand copies are deliberately not issued, so its stage wait runs out after about 2 s; the
+ * kernel records CUMF_ERR_TIMEOUT in *status_out, drains and frees its tensor memory, and an
+ * ordinary product on the same context is then checked.  *seconds (may be NULL) receives the
+ * timed-out launch's duration.  Returns CUMF_OK when the context stayed usable. */
+int cumf_selftest_wait_timeout(int *status_out, double *seconds);
+
 /* ---- checkpoint / resume (no reference counterpart) ---------------------------------- */
 /* Periodic checkpoints of a mode-A run (u = v = 1).  The file holds the factors exactly as
  * training keeps them in HBM (permuted rows, scaled, storage precision), the number of

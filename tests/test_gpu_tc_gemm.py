@@ -78,3 +78,15 @@ def test_tc_gemm_split_k_matches_torch_fp32(lib, cuda, M, N, K):
     exp = A.float() @ B.float().T
     scale = exp.abs().max().item()
     assert (out - exp).abs().max().item() <= 1e-4 * scale + 1e-6
+
+
+def test_wait_timeout_reports_status_and_context_survives(lib, cuda):
+    """A product whose operand copies are never issued (a flag nothing sets in normal use):
+    its stage wait runs out after about 2 s, the kernel reports CUMF_ERR_TIMEOUT, frees its
+    tensor memory and returns; the same context then computes an ordinary product."""
+    from cumf_sgd_gb300 import _lib
+    status, secs = C.c_int(0), C.c_double(0)
+    rc = lib.cumf_selftest_wait_timeout(C.byref(status), C.byref(secs))
+    assert rc == 0, lib.cumf_last_error()
+    assert status.value == _lib.CUMF_ERR_TIMEOUT
+    assert 1.5 <= secs.value <= 12.0
