@@ -54,6 +54,7 @@ class Parameter:
     ring: int = -1
     tail_epochs: int = 0
     tail_start: int = 0
+    deterministic: int = 0
 
     @property
     def ux(self) -> int:
@@ -68,7 +69,8 @@ class Parameter:
         _lib.check(_lib.load().cumf_default_params(C.byref(p)))
         for f in ("k", "num_workers", "u_grid", "v_grid", "x_grid", "y_grid", "num_iters", "gpu",
                   "lambda_p", "lambda_q", "lrate", "alpha", "beta", "seed", "lanes",
-                  "epochs_per_launch", "prefetch", "l2_hints", "ring", "tail_epochs", "tail_start"):
+                  "epochs_per_launch", "prefetch", "l2_hints", "ring", "tail_epochs", "tail_start",
+                  "deterministic"):
             setattr(p, f, getattr(self, f))
         p.precision = PRECISIONS[self.precision] if isinstance(self.precision, str) else int(self.precision)
         p.quiet = int(bool(self.quiet))
@@ -517,6 +519,21 @@ def sgd_train_ckpt(tr: MFProblem, te: Optional[MFProblem], param: Parameter, pat
     _lib.check(rc)
     stats = TrainStats(**{f: getattr(st, f) for f, _ in _lib.TrainStats._fields_ if f != "reserved_"})
     return MFModel(out), stats, done.value
+
+
+def dev_strata_layout(d_R: int, nnz: int, groups: int, d_out: int, d_block_off: int, stream: int = 0) -> None:
+    """Ratings stably sorted into the groups x groups blocks of the deterministic schedule."""
+    _lib.check(_lib.load().cumf_dev_strata_layout(d_R, nnz, groups, d_out, d_block_off, stream or None))
+
+
+def dev_strata_epochs(d_S: int, d_block_off: int, groups: int, d_P: int, m: int, d_Q: int, n: int, k: int,
+                      precision: str, lr: np.ndarray, first_epoch: int, n_epochs: int, lambda_p: float,
+                      lambda_q: float, seed: int, d_status: int = 0, stream: int = 0) -> None:
+    """Epochs of the deterministic stratified schedule on caller-owned device buffers."""
+    lr = np.ascontiguousarray(lr, dtype=np.float32)
+    _lib.check(_lib.load().cumf_dev_strata_epochs(d_S, d_block_off, groups, d_P, m, d_Q, n, k, PRECISIONS[precision],
+                                                  lr.ctypes.data, first_epoch, n_epochs, lambda_p, lambda_q, seed,
+                                                  d_status or None, stream or None))
 
 
 # ---- batched factorizations ------------------------------------------------------------

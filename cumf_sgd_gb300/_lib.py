@@ -45,7 +45,7 @@ class Params(C.Structure):
                 ("seed", C.c_uint64), ("precision", C.c_int32), ("lanes", C.c_int32),
                 ("quiet", C.c_int32), ("epochs_per_launch", C.c_int32),
                 ("verbose_epochs", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("ring", C.c_int32), ("tail_epochs", C.c_int32), ("reserved_", C.c_int32),
+                ("ring", C.c_int32), ("tail_epochs", C.c_int32), ("deterministic", C.c_int32),
                 ("tail_start", C.c_int64)]
 
 
@@ -102,6 +102,10 @@ _SIGS = {
     "cumf_train_ckpt": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Checkpoint),
                                   C.POINTER(Model), C.POINTER(TrainStats), C.POINTER(C.c_int32)]),
     "cumf_selftest_wait_timeout": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "cumf_dev_strata_layout": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cumf_dev_strata_epochs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int32, C.c_void_p,
+                                         C.c_int32, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_float,
+                                         C.c_float, C.c_uint64, C.c_void_p, C.c_void_p]),
     "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),

@@ -37,6 +37,7 @@ LIB_SOURCES = [
     "batch.cu",
     "text_parse.cu",
     "eval.cu",
+    "strata.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp", "cumf_transform": "transform_main.cpp"}
 

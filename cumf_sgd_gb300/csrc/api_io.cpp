@@ -246,6 +246,11 @@ int cumf_parse_args(int argc, char **argv, cumf_args *out) {
             p.lanes = atoi(argv[i]);
         } else if (a == "--quiet") {
             p.quiet = 1;
+        } else if (a == "--deterministic") {
+            if (!need(i, "need to specify a number after --deterministic")) return CUMF_ERR_ARG;
+            ++i;
+            if (!is_numerical(argv[i])) return fail(CUMF_ERR_ARG, "--deterministic should be followed by a number");
+            p.deterministic = atoi(argv[i]);
         } else {
             break;
         }

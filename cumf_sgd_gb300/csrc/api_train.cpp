@@ -156,6 +156,7 @@ int ckpt_read(const char *path, const CkptHeader &want, void *d_P, void *d_Q, un
     if (h.m != want.m || h.n != want.n || h.nnz != want.nnz || h.records_digest != want.records_digest)
         return bad("training ratings");
     if (h.tail_epochs != want.tail_epochs || h.tail_start != want.tail_start) return bad("fold-in epochs");
+    if (h.reserved != want.reserved) return bad("schedule (batch-Hogwild or deterministic grid)");
     if (h.bytes_p != want.bytes_p || h.bytes_q != want.bytes_q) return bad("factor sizes");
     if (h.epochs_done < 0 || h.epochs_done > want.num_iters) return bad("more epochs done than this run has");
     PinnedHost buf;
@@ -263,6 +264,17 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(d_lr.alloc(lr.size() * sizeof(float)));
     CUMF_CUDA(cudaMemcpyAsync(d_lr.p, lr.data(), lr.size() * sizeof(float), cudaMemcpyHostToDevice, s));
 
+    // Deterministic schedule: the shuffled, scaled ratings stably sorted into G x G blocks.
+    const int strata_g = p.deterministic > 0 ? strata_groups(nnz, p.deterministic) : 0;
+    DevBuf d_S, d_off;
+    if (strata_g > 0 && nnz > 0) {
+        CUMF_CUDA(d_S.alloc((size_t)nnz * sizeof(cumf_node)));
+        CUMF_CUDA(d_off.alloc(((size_t)strata_g * strata_g + 1) * sizeof(unsigned long long)));
+        if (int rc = strata_layout(d_R.as<cumf_node>(), nnz, strata_g, d_S.as<cumf_node>(),
+                                   d_off.as<unsigned long long>(), s))
+            return rc;
+    }
+
     const float factor = (float)sqrt(pr.scale);  // scale_model (sgd.cu:598)
     // model->b (sgd.cu:679); an empty problem (0 / 0 in the reference) gets b = 0.
     const float b = nnz ? pr.ave / pr.std_dev : 0.f;
@@ -306,6 +318,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         ckh.m = m;
         ckh.n = n;
         ckh.tail_epochs = p.tail_epochs;
+        ckh.reserved = strata_g;  // the deterministic schedule's grid (0: batch-Hogwild)
         ckh.seed = p.seed;
         ckh.lambda_p = p.lambda_p;
         ckh.lambda_q = p.lambda_q;
@@ -351,9 +364,17 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         tu.hints = p.l2_hints;
         tu.ring = p.ring;
         tu.freeze_q = (tail && ep < p.tail_epochs) ? 1 : 0;  // fold-in: items stay as given
-        CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m, d_Q.p, n, k, p.precision, workers_ep, tu,
-                                    d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
-                                    &lanes_used));
+        if (strata_g > 0) {
+            if (nnz > 0)
+                if (int rc = strata_epochs(d_S.as<cumf_node>(), d_off.as<unsigned long long>(), strata_g, d_P.p, m,
+                                           d_Q.p, n, k, p.precision, lr.data(), ep, cnt, lambda_p, lambda_q, p.seed,
+                                           d_status.as<int>(), s))
+                    return rc;
+        } else {
+            CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m, d_Q.p, n, k, p.precision, workers_ep, tu,
+                                        d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
+                                        &lanes_used));
+        }
         float ms = 0;
         if (sync_each) {
             CUMF_CUDA(cudaEventRecord(e1.e, s));
@@ -431,7 +452,7 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         st->mean = pr.ave;
         st->std_dev = pr.std_dev;
         st->mode = 0;
-        st->num_workers = workers;
+        st->num_workers = strata_g > 0 ? strata_g : workers;  // deterministic: workers per stratum
         st->lanes = lanes_used;
     }
     if (!p.quiet) {

@@ -3,14 +3,15 @@
 //   cumf_sgd [-g id] [-l lp[,lq]] [-k 128] [-t iters] [-r lrate] [-a alpha] [-b beta]
 //            [-s workers] [-u U] [-v V] [-x X] [-y Y] [-p test_file]
 //            [--seed N] [--precision fp16|bf16|fp32|bf16sr|fp16sr] [--lanes N] [--quiet]
-//            [--checkpoint path [--checkpoint-every N] [--resume]]
+//            [--checkpoint path [--checkpoint-every N] [--resume]] [--deterministic G]
 //            train_file [model_file]
 //
 // Exit status 1 on bad arguments (main.cpp:286-289); unlike the reference, a failed read,
 // training or model write also exits non-zero with the library's message.  With -p the
 // test RMSE is printed after each epoch (the reference parses -p but never reads it).
 // --checkpoint writes the in-HBM factors every N epochs (default 1; mode A only) and
-// --resume continues from a matching checkpoint (cumf_train_ckpt).
+// --resume continues from a matching checkpoint (cumf_train_ckpt).  --deterministic 1 (or a
+// grid size G) trains with the bit-reproducible stratified schedule instead of batch-Hogwild.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>

@@ -96,6 +96,18 @@ void parallel_chunks(int64_t n, F f) {
 // records, without moving them: each step reads one block id and writes one index.
 void grid_order(const int32_t *bid, int64_t nnz, int G, const int64_t *grid_size, int64_t *fin);
 
+// ---- strata.cu (deterministic training) ---------------------------------------------------
+// Groups per side of the stratified grid: `requested` when > 1, else about sqrt(nnz / 24).
+int strata_groups(int64_t nnz, int requested);
+// d_out: the ratings stably sorted by block (u mod G) * G + (v mod G); d_block_off: G*G + 1
+// block offsets.  Synchronises the stream.
+int strata_layout(const cumf_node *d_R, int64_t nnz, int G, cumf_node *d_out, unsigned long long *d_block_off,
+                  cudaStream_t s);
+// Epochs [first_epoch, first_epoch + n_epochs): G strata each, learning rates h_lr[epoch] (host).
+int strata_epochs(const cumf_node *d_S, const unsigned long long *d_block_off, int G, void *d_P, int32_t m,
+                  void *d_Q, int32_t n, int k, int precision, const float *h_lr, int first_epoch, int n_epochs,
+                  float lambda_p, float lambda_q, uint64_t seed, int *d_status, cudaStream_t s);
+
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }
 

@@ -64,6 +64,12 @@ inline int check_params(const cumf_params *p) {
     if (p->u_grid < 1 || p->v_grid < 1 || p->x_grid < 1 || p->y_grid < 1)
         return fail(CUMF_ERR_ARG, "grid sizes must be positive");
     if (p->precision < CUMF_FP16 || p->precision > CUMF_FP16_SR) return fail(CUMF_ERR_ARG, "unknown precision");
+    if (p->deterministic < 0 || p->deterministic > 4096)
+        return fail(CUMF_ERR_ARG, "deterministic must be 0 (batch-Hogwild), 1 (automatic grid) or a grid of 2..4096");
+    if (p->deterministic > 0 && p->u_grid * p->v_grid != 1)
+        return fail(CUMF_ERR_ARG, "the deterministic schedule needs u = v = 1 (the whole problem in HBM)");
+    if (p->deterministic > 0 && p->tail_epochs > 0)
+        return fail(CUMF_ERR_ARG, "the deterministic schedule has no fold-in epochs");
     if (p->lanes != 0 && !lanes_supported(p->k, p->precision, p->lanes))
         return fail(CUMF_ERR_ARG, "unsupported lane count " + std::to_string(p->lanes) + " for k=" + std::to_string(p->k));
     return CUMF_OK;

@@ -103,8 +103,11 @@ typedef struct cumf_params {
     int32_t l2_hints;      /* L2 eviction hints: -1 = tuned default, 0 = off, 1 = on      */
     int32_t ring;          /* update kernel pipeline (see cumf_tuning.ring)               */
     int32_t tail_epochs;   /* the first tail_epochs epochs sample only records            */
-    int32_t reserved_;     /*   [tail_start, nnz) (e.g. newly added users' ratings) and     */
-    int64_t tail_start;    /*   update user rows only (item rows frozen), then all records */
+    int32_t deterministic; /* 0 = batch-Hogwild (the reference); 1 = the stratified schedule
+                              of cumf_dev_strata_epochs, bit-reproducible (mode A), with an
+                              automatic grid; > 1 = that many user / item groups            */
+    int64_t tail_start;    /* (tail_epochs) [tail_start, nnz) (e.g. newly added users'
+                              ratings): those epochs update user rows only (item rows frozen) */
 } cumf_params;
 
 /* Launch tuning of the update kernel (the knobs the autotuner searches). */
@@ -382,6 +385,22 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
  * ordinary product on the same context is then checked.  *seconds (may be NULL) receives the
  * timed-out launch's duration.  Returns CUMF_OK when the context stayed usable. */
 int cumf_selftest_wait_timeout(int *status_out, double *seconds);
+
+/* ---- deterministic schedule (no reference counterpart) -------------------------------- */
+/* Stratified SGD: ratings bucketed into a G x G grid of blocks (user group u mod G, item group
+ * v mod G, stable order inside a block); stratum s of an epoch updates the blocks
+ * (a, (a + s) mod G), which share no user and no item, one worker per block, so the result is
+ * the same on every run and equals the serial restatement bit for bit.  The per-rating
+ * update is the batch-Hogwild kernel's (warp32.h:85-99; stochastic rounding keyed by the
+ * rating's position in the sorted array). */
+/* d_out (nnz records) and d_block_off (groups*groups + 1 offsets) receive the layout. */
+int cumf_dev_strata_layout(const cumf_node *d_R, int64_t nnz, int groups, cumf_node *d_out,
+                           unsigned long long *d_block_off, void *stream);
+/* Epochs over the layout; h_lr is a host array indexed by epoch. */
+int cumf_dev_strata_epochs(const cumf_node *d_S, const unsigned long long *d_block_off, int groups, void *d_P,
+                           int32_t m, void *d_Q, int32_t n, int k, int precision, const float *h_lr,
+                           int first_epoch, int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
+                           int *d_status, void *stream);
 
 /* ---- checkpoint / resume (no reference counterpart) ---------------------------------- */
 /* Periodic checkpoints of a mode-A run (u = v = 1).  The file holds the factors exactly as

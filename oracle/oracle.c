@@ -795,3 +795,43 @@ double or_evaluate(const or_node *R, int64_t nnz, int32_t prob_m, int32_t prob_n
     }
     return criterion == 0 ? sqrt(acc / (double)nnz) : acc / (double)nnz;
 }
+
+
+/* ---- deterministic stratified schedule --------------------------------------------------- */
+
+int64_t or_strata_epochs(const or_node *R, int64_t nnz, float *P, int32_t m, float *Q, int32_t n, int k, int kind,
+                         int sr, int lanes, int G, const float *lr, int first_epoch, int n_epochs, float lambda_p,
+                         float lambda_q, uint64_t seed) {
+    const int64_t blocks = (int64_t)G * G;
+    int64_t *off = (int64_t *)calloc((size_t)blocks + 1, sizeof(int64_t));
+    or_node *S = (or_node *)malloc((size_t)(nnz ? nnz : 1) * sizeof(or_node));
+    for (int64_t i = 0; i < nnz; ++i) off[((uint32_t)R[i].u % (uint32_t)G) * (uint32_t)G + (uint32_t)R[i].v % (uint32_t)G + 1]++;
+    for (int64_t b = 0; b < blocks; ++b) off[b + 1] += off[b];
+    int64_t *fill = (int64_t *)malloc((size_t)blocks * sizeof(int64_t));
+    memcpy(fill, off, (size_t)blocks * sizeof(int64_t));
+    for (int64_t i = 0; i < nnz; ++i)  /* stable counting sort */
+        S[fill[((uint32_t)R[i].u % (uint32_t)G) * (uint32_t)G + (uint32_t)R[i].v % (uint32_t)G]++] = R[i];
+    int64_t skipped = 0;
+    for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
+        const uint32_t round_key = (uint32_t)(or_splitmix64(seed ^ (0x5352ull << 48)) + (uint64_t)ep);
+        for (int st = 0; st < G; ++st) {
+            for (int a = 0; a < G; ++a) {
+                const int64_t blk = (int64_t)a * G + (a + st) % G;
+                for (int64_t i = off[blk]; i < off[blk + 1]; ++i) {
+                    const or_node x = S[i];
+                    if ((uint32_t)x.u >= (uint32_t)m || (uint32_t)x.v >= (uint32_t)n) {
+                        ++skipped;
+                        continue;
+                    }
+                    const uint32_t key = sr ? (round_key ^ or_lowbias32((uint32_t)i)) : 0u;
+                    update_rows(P + (int64_t)x.u * k, Q + (int64_t)x.v * k, k, x.r, lr[ep], lambda_p, lambda_q, kind,
+                                sr, key, lanes, OR_DOT_LANES);
+                }
+            }
+        }
+    }
+    free(off);
+    free(fill);
+    free(S);
+    return skipped;
+}

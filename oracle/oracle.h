@@ -150,6 +150,15 @@ void or_sgd_epochs_f64_threads(or_sgd64_args *a, int threads);
 double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t m, const double *Q,
                         int32_t n, int k, double b);
 
+/* The deterministic stratified schedule (the library's strata.cu): records stably sorted by
+ * block (u mod G) * G + (v mod G); epoch ep runs strata s = 0 .. G-1, each the blocks
+ * (a, (a + s) mod G) in any order (they share no rows), each block's records in order, with
+ * the kernel's update (OR_DOT_LANES over `lanes`; stochastic rounding keyed by the record's
+ * position in the sorted array).  Returns the number of records skipped as out of range. */
+int64_t or_strata_epochs(const or_node *R, int64_t nnz, float *P, int32_t m, float *Q, int32_t n, int k, int kind,
+                         int sr, int lanes, int G, const float *lr, int first_epoch, int n_epochs, float lambda_p,
+                         float lambda_q, uint64_t seed);
+
 /* data/netflix/transform.cpp:31-42 (the strict form the GPU converter implements): skips
  * `header_lines` lines as fscanf(f, "%[^\n]\n") does, then reads whitespace-separated
  * triples, u and v with strtol (the conversion behind %d) and r with strtof (behind %f).

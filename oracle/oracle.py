@@ -124,6 +124,10 @@ def lib() -> C.CDLL:
         _lib.or_evaluate.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                      C.c_void_p, C.c_int32, C.c_int, C.c_float, C.c_int]
         _lib.or_evaluate.restype = C.c_double
+        _lib.or_strata_epochs.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                          C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                          C.c_int, C.c_float, C.c_float, C.c_uint64]
+        _lib.or_strata_epochs.restype = C.c_int64
         _lib.or_parse_text.argtypes = [C.c_char_p, C.c_int64, C.c_int, C.c_void_p, C.c_int64,
                                         C.POINTER(C.c_int64)]
         _lib.or_parse_text.restype = C.c_int64
@@ -363,3 +367,13 @@ def ref_criteria(test_path: str, model_path: str) -> dict:
             _, c, v = line.split()
             out[int(c)] = float(v)
     return out
+
+
+def strata_epochs(records: np.ndarray, P: np.ndarray, Q: np.ndarray, precision: str, groups: int, lr: np.ndarray,
+                  first_epoch: int, n_epochs: int, lambda_p: float, lambda_q: float, seed: int, lanes: int) -> int:
+    """The deterministic stratified schedule on float32 P, Q in place; returns skipped records."""
+    kind, sr = KIND[precision]
+    rec = np.ascontiguousarray(records)
+    lr = np.ascontiguousarray(lr, dtype=np.float32)
+    return lib().or_strata_epochs(_ptr(rec), len(rec), _ptr(P), P.shape[0], _ptr(Q), Q.shape[0], P.shape[1], kind, sr,
+                                  lanes, groups, _ptr(lr), first_epoch, n_epochs, lambda_p, lambda_q, seed)
