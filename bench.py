@@ -686,19 +686,21 @@ def run_streamed_suite(args):
     tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"], m=m, n=n)
     sm, _, _ = cm.device_info(0)
     epochs = max(1, min(args.steps, 20))
-    for grid in [(1, 1, 1, 1), (2, 2, 1, 1), (4, 1, 1, 1), (2, 1, 2, 2), (2, 2, 2, 2)]:
-        u, v, x, y = grid
+    for grid in [(1, 1, 1, 1), "deterministic", (2, 2, 1, 1), (4, 1, 1, 1), (2, 1, 2, 2), (2, 2, 2, 2)]:
+        det = grid == "deterministic"
+        u, v, x, y = (1, 1, 1, 1) if det else grid
         blocks = u * v * x * y
         workers = cm.auto_workers(max(1, nnz // blocks), sm, K, "fp16", 0)
         par = cm.Parameter(k=K, num_workers=workers, num_iters=epochs, lambda_p=0.05, lambda_q=0.05, alpha=0.08,
-                           beta=0.3, seed=0, gpu=0, precision="fp16", u_grid=u, v_grid=v, x_grid=x, y_grid=y, quiet=1)
+                           beta=0.3, seed=0, gpu=0, precision="fp16", u_grid=u, v_grid=v, x_grid=x, y_grid=y, quiet=1,
+                           deterministic=int(det))
         cm.sgd_train(prob, None, cm.Parameter(**{**par.__dict__, "num_iters": 1}))  # warm-up
         t0 = time.perf_counter()
         model, st = cm.sgd_train(prob, None, par, with_stats=True)
         wall = time.perf_counter() - t0
         rmse = cm.calc_rmse(tprob, model)
-        mode = "ABC"[st.mode]
-        print(json.dumps({"suite": "streamed", "mode": mode, "u_v_x_y": grid, "workers_per_block": workers,
+        mode = "A, deterministic" if det else "ABC"[st.mode]
+        print(json.dumps({"suite": "streamed", "mode": mode, "u_v_x_y": (u, v, x, y), "workers_per_block": st.num_workers,
                           "epochs": epochs, "train_ms": st.train_ms, "updates_per_sec": nnz * epochs / (st.train_ms * 1e-3),
                           "wall_s": wall, "prep_ms": st.prep_ms, "export_ms": st.export_ms,
                           "test_rmse": rmse}), flush=True)
