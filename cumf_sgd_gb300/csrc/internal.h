@@ -97,6 +97,8 @@ void parallel_chunks(int64_t n, F f) {
 void grid_order(const int32_t *bid, int64_t nnz, int G, const int64_t *grid_size, int64_t *fin);
 
 // ---- strata.cu (deterministic training) ---------------------------------------------------
+// The strata of epoch ep in their seeded random order (a permutation of 0 .. G-1).
+void strata_order(uint64_t seed, int ep, int G, int *order);
 // Groups per side of the stratified grid: `requested` when > 1, else about sqrt(nnz / 24).
 int strata_groups(int64_t nnz, int requested);
 // d_out: the ratings stably sorted by block (u mod G) * G + (v mod G); d_block_off: G*G + 1

@@ -3,8 +3,8 @@
 // Batch-Hogwild (sgd_update.cu) lets thousands of workers update shared rows without locks,
 // so results vary from run to run.  With `deterministic` set, the shuffled ratings are
 // bucketed into a G x G grid of blocks (user group u mod G, item group v mod G) and an epoch
-// runs G strata: stratum s holds the blocks (a, (a + s) mod G) for a = 0 .. G-1, which share
-// no user and no item, so G workers update them in parallel without any row in common and
+// runs the G strata in a seeded random order: stratum s holds the blocks (a, (a + s) mod G)
+// for a = 0 .. G-1, which share no user and no item, so G workers update them in parallel without any row in common and
 // the result is the same on every run and equal to the serial restatement.  Within a block the
 // ratings keep their input order (a stable sort).  The per-rating arithmetic is the update of
 // singleGPU/sgd_k128_kernel_hogwild_warp32.h:85-99 exactly as the batch-Hogwild kernel does it
@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "cumf_sgd.h"
 #include "device_common.cuh"
@@ -137,6 +138,20 @@ StratumFn pick(int precision, int *lanes) {
 
 }  // namespace
 
+// The strata of epoch ep in a seeded random order: Fisher-Yates over 0 .. G-1 drawing
+// splitmix64(seed ^ tag, epoch, step) mod (step + 1).
+void strata_order(uint64_t seed, int ep, int G, int *order) {
+    for (int i = 0; i < G; ++i) order[i] = i;
+    uint64_t h = splitmix64(seed ^ (0x5354ull << 48)) + (uint64_t)ep * 0x9E3779B97F4A7C15ull;
+    for (int i = G - 1; i > 0; --i) {
+        h = splitmix64(h);
+        const int j = (int)(h % (uint64_t)(i + 1));
+        const int t = order[i];
+        order[i] = order[j];
+        order[j] = t;
+    }
+}
+
 int strata_groups(int64_t nnz, int requested) {
     if (requested > 1) return requested;
     // About 24 ratings per block: G^2 blocks, G workers per stratum.
@@ -200,11 +215,13 @@ int strata_epochs(const cumf_node *d_S, const unsigned long long *d_block_off, i
     }
     const int groups_per_block = kST / lanes;
     const int blocks = (G + groups_per_block - 1) / groups_per_block;
+    std::vector<int> order(G);
     for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
         const uint32_t round_key = (uint32_t)(splitmix64(seed ^ (kTagRound << 48)) + (uint64_t)ep);
-        for (int st = 0; st < G; ++st)
-            fn<<<blocks, kST, 0, s>>>(d_S, d_block_off, G, st, d_P, d_Q, (uint32_t)m, (uint32_t)n, h_lr[ep], lambda_p,
-                                      lambda_q, round_key, d_status);
+        strata_order(seed, ep, G, order.data());
+        for (int j = 0; j < G; ++j)
+            fn<<<blocks, kST, 0, s>>>(d_S, d_block_off, G, order[j], d_P, d_Q, (uint32_t)m, (uint32_t)n, h_lr[ep],
+                                      lambda_p, lambda_q, round_key, d_status);
         CUMF_CUDA(cudaGetLastError());
     }
     return CUMF_OK;

@@ -388,8 +388,8 @@ int cumf_selftest_wait_timeout(int *status_out, double *seconds);
 
 /* ---- deterministic schedule (no reference counterpart) -------------------------------- */
 /* Stratified SGD: ratings bucketed into a G x G grid of blocks (user group u mod G, item group
- * v mod G, stable order inside a block); stratum s of an epoch updates the blocks
- * (a, (a + s) mod G), which share no user and no item, one worker per block, so the result is
+ * v mod G, stable order inside a block); an epoch runs the G strata in a seeded random order,
+ * stratum s updating the blocks (a, (a + s) mod G), which share no user and no item, one worker per block, so the result is
  * the same on every run and equals the serial restatement bit for bit.  The per-rating
  * update is the batch-Hogwild kernel's (warp32.h:85-99; stochastic rounding keyed by the
  * rating's position in the sorted array). */

@@ -812,9 +812,21 @@ int64_t or_strata_epochs(const or_node *R, int64_t nnz, float *P, int32_t m, flo
     for (int64_t i = 0; i < nnz; ++i)  /* stable counting sort */
         S[fill[((uint32_t)R[i].u % (uint32_t)G) * (uint32_t)G + (uint32_t)R[i].v % (uint32_t)G]++] = R[i];
     int64_t skipped = 0;
+    int *order = (int *)malloc((size_t)G * sizeof(int));
     for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
         const uint32_t round_key = (uint32_t)(or_splitmix64(seed ^ (0x5352ull << 48)) + (uint64_t)ep);
-        for (int st = 0; st < G; ++st) {
+        /* strata in a seeded random order: Fisher-Yates with splitmix64 draws */
+        for (int i = 0; i < G; ++i) order[i] = i;
+        uint64_t h = or_splitmix64(seed ^ (0x5354ull << 48)) + (uint64_t)ep * 0x9E3779B97F4A7C15ull;
+        for (int i = G - 1; i > 0; --i) {
+            h = or_splitmix64(h);
+            const int j = (int)(h % (uint64_t)(i + 1));
+            const int t = order[i];
+            order[i] = order[j];
+            order[j] = t;
+        }
+        for (int oi = 0; oi < G; ++oi) {
+            const int st = order[oi];
             for (int a = 0; a < G; ++a) {
                 const int64_t blk = (int64_t)a * G + (a + st) % G;
                 for (int64_t i = off[blk]; i < off[blk + 1]; ++i) {
@@ -830,6 +842,7 @@ int64_t or_strata_epochs(const or_node *R, int64_t nnz, float *P, int32_t m, flo
             }
         }
     }
+    free(order);
     free(off);
     free(fill);
     free(S);

@@ -151,7 +151,8 @@ double or_calc_rmse_f64(const or_node *R, int64_t nnz, const double *P, int32_t 
                         int32_t n, int k, double b);
 
 /* The deterministic stratified schedule (the library's strata.cu): records stably sorted by
- * block (u mod G) * G + (v mod G); epoch ep runs strata s = 0 .. G-1, each the blocks
+ * block (u mod G) * G + (v mod G); epoch ep runs the strata in a seeded random order
+ * (Fisher-Yates over 0 .. G-1 with splitmix64 draws), stratum s being the blocks
  * (a, (a + s) mod G) in any order (they share no rows), each block's records in order, with
  * the kernel's update (OR_DOT_LANES over `lanes`; stochastic rounding keyed by the record's
  * position in the sorted array).  Returns the number of records skipped as out of range. */
