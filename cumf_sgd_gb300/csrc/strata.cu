@@ -64,59 +64,89 @@ __global__ void __launch_bounds__(kST) stratum_kernel(const cumf_node *__restric
     uint4 *const P = reinterpret_cast<uint4 *>(Pv) + lane * NV;
     uint4 *const Q = reinterpret_cast<uint4 *>(Qv) + lane * NV;
     const uint64_t pol = l2_policy(true, true);
+    const unsigned long long i0 = block_off[blk], i1 = block_off[blk + 1];
     int bad = 0;
-    for (unsigned long long i = block_off[blk]; i < block_off[blk + 1]; ++i) {
-        const cumf_node x = R[i];
-        const uint32_t u = (uint32_t)x.u, v = (uint32_t)x.v;
-        if (u >= m || v >= n) {
-            bad = 1;
-            continue;
-        }
-        uint4 fp[NV], fq[NV];
+    if (i0 >= i1) return;
+    // One-deep pipeline: the rows of rating i+1 are loaded while rating i is computed; when
+    // rating i+1 reuses a row that rating i has just written, the fresh values are forwarded,
+    // so the block's ratings are applied strictly in order.
+    cumf_node x = R[i0];
+    bool ok = ((uint32_t)x.u < m) & ((uint32_t)x.v < n);
+    uint4 fp[NV], fq[NV];
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+        fp[w] = ok ? ld_row_hint(P + (uint64_t)(uint32_t)x.u * ROW_WORDS + w, pol) : make_uint4(0, 0, 0, 0);
+        fq[w] = ok ? ld_row_hint(Q + (uint64_t)(uint32_t)x.v * ROW_WORDS + w, pol) : make_uint4(0, 0, 0, 0);
+    }
+    for (unsigned long long i = i0; i < i1; ++i) {
+        const bool has_next = i + 1 < i1;
+        const cumf_node xn = has_next ? R[i + 1] : x;
+        const bool okn = has_next && ((uint32_t)xn.u < m) & ((uint32_t)xn.v < n);
+        uint4 np[NV], nq[NV];
 #pragma unroll
         for (int w = 0; w < NV; ++w) {
-            fp[w] = ld_row_hint(P + (uint64_t)u * ROW_WORDS + w, pol);
-            fq[w] = ld_row_hint(Q + (uint64_t)v * ROW_WORDS + w, pol);
+            np[w] = okn ? ld_row_hint(P + (uint64_t)(uint32_t)xn.u * ROW_WORDS + w, pol) : make_uint4(0, 0, 0, 0);
+            nq[w] = okn ? ld_row_hint(Q + (uint64_t)(uint32_t)xn.v * ROW_WORDS + w, pol) : make_uint4(0, 0, 0, 0);
         }
-        float s = 0.f;
+        if (ok) {
+            const uint32_t u = (uint32_t)x.u, v = (uint32_t)x.v;
+            float sdot = 0.f;
 #pragma unroll
-        for (int w = 0; w < NV; ++w) {
+            for (int w = 0; w < NV; ++w) {
 #pragma unroll
-            for (int h = 0; h < C::kPairs; ++h) {
-                const float2 pp = C::get(fp[w], h), qq = C::get(fq[w], h);
-                s = __fmaf_rn(pp.x, qq.x, s);
-                s = __fmaf_rn(pp.y, qq.y, s);
-            }
-        }
-#pragma unroll
-        for (int o = L / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
-        const float err = x.r - s;
-        const uint32_t key = SR ? (round_key ^ lowbias32((uint32_t)i)) : 0u;
-        uint4 wp[NV], wq[NV];
-#pragma unroll
-        for (int w = 0; w < NV; ++w) {
-#pragma unroll
-            for (int h = 0; h < C::kPairs; ++h) {
-                const float2 pp = C::get(fp[w], h), qq = C::get(fq[w], h);
-                const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
-                const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
-                const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
-                const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
-                if (SR) {
-                    const uint32_t pair = (uint32_t)(((lane * NV + w) * C::kPairs + h) * 2);
-                    C::put_sr(wp[w], h, px, py, lowbias32(key + pair));
-                    C::put_sr(wq[w], h, qx, qy, lowbias32(key + pair + 1u));
-                } else {
-                    C::put(wp[w], h, px, py);
-                    C::put(wq[w], h, qx, qy);
+                for (int h = 0; h < C::kPairs; ++h) {
+                    const float2 pp = C::get(fp[w], h), qq = C::get(fq[w], h);
+                    sdot = __fmaf_rn(pp.x, qq.x, sdot);
+                    sdot = __fmaf_rn(pp.y, qq.y, sdot);
                 }
             }
+#pragma unroll
+            for (int o = L / 2; o >= 1; o >>= 1) sdot += __shfl_xor_sync(gmask, sdot, o);
+            const float err = x.r - sdot;
+            const uint32_t key = SR ? (round_key ^ lowbias32((uint32_t)i)) : 0u;
+            uint4 wp[NV], wq[NV];
+#pragma unroll
+            for (int w = 0; w < NV; ++w) {
+#pragma unroll
+                for (int h = 0; h < C::kPairs; ++h) {
+                    const float2 pp = C::get(fp[w], h), qq = C::get(fq[w], h);
+                    const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
+                    const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
+                    const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
+                    const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
+                    if (SR) {
+                        const uint32_t pair = (uint32_t)(((lane * NV + w) * C::kPairs + h) * 2);
+                        C::put_sr(wp[w], h, px, py, lowbias32(key + pair));
+                        C::put_sr(wq[w], h, qx, qy, lowbias32(key + pair + 1u));
+                    } else {
+                        C::put(wp[w], h, px, py);
+                        C::put(wq[w], h, qx, qy);
+                    }
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < NV; ++w) {
+                st_row_hint(P + (uint64_t)u * ROW_WORDS + w, wp[w], pol);
+                st_row_hint(Q + (uint64_t)v * ROW_WORDS + w, wq[w], pol);
+            }
+            if (okn && (uint32_t)xn.u == u) {
+#pragma unroll
+                for (int w = 0; w < NV; ++w) np[w] = wp[w];
+            }
+            if (okn && (uint32_t)xn.v == v) {
+#pragma unroll
+                for (int w = 0; w < NV; ++w) nq[w] = wq[w];
+            }
+        } else {
+            bad = 1;
         }
 #pragma unroll
         for (int w = 0; w < NV; ++w) {
-            st_row_hint(P + (uint64_t)u * ROW_WORDS + w, wp[w], pol);
-            st_row_hint(Q + (uint64_t)v * ROW_WORDS + w, wq[w], pol);
+            fp[w] = np[w];
+            fq[w] = nq[w];
         }
+        x = xn;
+        ok = okn;
     }
     if (bad && status != nullptr && lane == 0) atomicExch(status, (int)CUMF_ERR_RANGE);
 }
