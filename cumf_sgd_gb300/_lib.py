@@ -106,6 +106,7 @@ _SIGS = {
     "cumf_dev_strata_epochs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int32, C.c_void_p,
                                          C.c_int32, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_float,
                                          C.c_float, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "cumf_probe_copy_bandwidth": (C.c_int, [C.c_int64, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
     "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),

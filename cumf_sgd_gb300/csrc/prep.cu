@@ -11,6 +11,7 @@
 // All are HBM-streaming kernels (grid-stride, coalesced); the reductions are two-pass with a
 // fixed grid so results do not depend on scheduling.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <math.h>
 #include <stdint.h>
 
@@ -199,6 +200,20 @@ __global__ void digest_kernel(const uint32_t *w, uint64_t nwords, unsigned long 
     if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
 }
 
+// `passes` copies of a[0..n16) to b within one launch, loads through L2 only (ld.global.cg),
+// each thread on the same 16-byte words every pass: with a and b small enough, every pass
+// after the first is served by L2.
+__global__ void copy_passes_kernel(const uint4 *__restrict__ a, uint4 *__restrict__ b, uint64_t n16, int passes) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int p = 0; p < passes; ++p) {
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16; i += stride) {
+            uint4 v = __ldcg(a + i);
+            v.x += (uint32_t)p;  // keeps every pass's copy live
+            b[i] = v;
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_digest(const void *d, uint64_t bytes, unsigned long long *d_out, cudaStream_t s) {
@@ -293,3 +308,36 @@ cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, 
 }
 
 }  // namespace cumf
+
+extern "C" int cumf_probe_copy_bandwidth(int64_t bytes, int passes, double *gbs, void *stream) {
+    using namespace cumf;
+    if (bytes < 16 || passes < 1 || !gbs) return fail(CUMF_ERR_ARG, "probe_copy_bandwidth: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint64_t n16 = (uint64_t)bytes / 16;
+    void *buf = nullptr;
+    CUMF_CUDA(cudaMalloc(&buf, n16 * 32));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMemsetAsync(buf, 1, n16 * 32, s);
+    const uint4 *a = static_cast<const uint4 *>(buf);
+    uint4 *b = static_cast<uint4 *>(buf) + n16;
+    int dev = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::max(1, sms) * 8;
+    if (e == cudaSuccess) copy_passes_kernel<<<grid, 256, 0, s>>>(a, b, n16, 2);  // warm: both buffers in cache
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) copy_passes_kernel<<<grid, 256, 0, s>>>(a, b, n16, passes);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "probe_copy_bandwidth");
+    *gbs = ms > 0 ? 2.0 * (double)n16 * 16.0 * passes / (ms * 1e-3) / 1e9 : 0.0;
+    return CUMF_OK;
+}

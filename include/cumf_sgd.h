@@ -379,6 +379,12 @@ int cumf_train_ex(const cumf_problem *tr, const cumf_problem *te, const cumf_par
                   const cumf_model *init, cumf_model *out, cumf_train_stats *stats, double *epoch_rmse,
                   double *epoch_ms);
 
+/* Diagnostic (no reference counterpart): copy bandwidth (bytes read + written per second, GB/s)
+ * of `passes` copies of a `bytes` buffer inside one launch, loads through L2 only.  With a
+ * working set well inside L2 (e.g. 2 x 32 MB) it measures the L2-resident copy rate used as a
+ * second roofline for the update kernel; with a large buffer, the HBM copy rate. */
+int cumf_probe_copy_bandwidth(int64_t bytes, int passes, double *gbs, void *stream);
+
 /* Self-test of the bounded waits (no reference counterpart): one tensor-core product whose
  * operand copies are deliberately not issued, so its stage wait runs out after about 2 s; the
  * kernel records CUMF_ERR_TIMEOUT in *status_out, drains and frees its tensor memory, and an
