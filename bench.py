@@ -72,9 +72,10 @@ def max_over_ranks(value: float, world: int) -> float:
     return float(t.item())
 
 
-def l2_copy_gbs(bytes_each: int = 32 << 20, passes: int = 200) -> float:
-    """L2-resident copy bandwidth (bytes read + written): `passes` copies of a 32 MB buffer
-    into another inside one launch (cumf_probe_copy_bandwidth), 64 MB in all on a 129 MB L2."""
+def l2_copy_gbs(bytes_each: int = 16 << 20, passes: int = 400) -> float:
+    """L2-resident copy bandwidth (bytes read + written): `passes` copies of a 16 MB buffer
+    into another inside one launch (cumf_probe_copy_bandwidth).  Measured on GB300: 12.3-13.9
+    TB/s for 8-48 MB buffers, 9.4 TB/s at 64 MB (spilling), 6.5-6.6 TB/s at 1-4 GB (HBM)."""
     import ctypes as C
     from cumf_sgd_gb300 import _lib
     out = C.c_double(0)
@@ -894,7 +895,7 @@ def main():
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(),
                              "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
                 "l2_roofline": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
-                                "peak_kind": "L2-resident copy (2 x 32 MB, 200 passes in one launch), measured in this run"},
+                                "peak_kind": "L2-resident copy (2 x 16 MB, 400 passes in one launch), measured in this run"},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu,
                 "time_to_target": ttt}
         print(json.dumps(line), flush=True)
