@@ -103,3 +103,15 @@ def test_zero_workers_means_automatic(lib, cuda):
         _, st = cm.sgd_train(prob, None, par, with_stats=True)
         blocks = grid[0] * grid[1]
         assert st.num_workers == cm.auto_workers(nnz // blocks, sm, 64, "fp16", 0)
+
+
+def test_copy_bandwidth_probe(lib, cuda):
+    """The roofline probe: an L2-resident copy is faster than one that streams from HBM."""
+    import ctypes as C
+    from cumf_sgd_gb300 import _lib
+    l2, hbm = C.c_double(0), C.c_double(0)
+    _lib.check(lib.cumf_probe_copy_bandwidth(16 << 20, 200, C.byref(l2), None))
+    _lib.check(lib.cumf_probe_copy_bandwidth(1 << 30, 3, C.byref(hbm), None))
+    assert hbm.value > 1000 and l2.value > 1.3 * hbm.value
+    with pytest.raises(cm.CumfError):
+        _lib.check(lib.cumf_probe_copy_bandwidth(8, 1, C.byref(l2), None))
