@@ -1,6 +1,6 @@
 """Benchmark of the batch-Hogwild SGD path (one JSON line on rank 0).
 
-Workload (BASELINE config 2): planted-model matrix 480,189 x 17,770 with 99,072,112 train
+Workload (the c2 shape): planted-model matrix 480,189 x 17,770 with 99,072,112 train
 ratings, k = 128, fp16 factors, 20 epochs, synthetic (seeded) in place of Netflix.
   value  updates/s = nnz * epochs / time, epochs run on device-resident data (one epoch =
          one step = one kernel launch), CUDA events on the launching stream;
@@ -212,7 +212,7 @@ def run_reference_arm(args):
 
 
 def run_precision_suite(args):
-    """Precision sweep (BASELINE config 3): c3 planted matrix 1,000,990 x 624,961, 252.8M
+    """Precision sweep (the c3 shape): planted matrix 1,000,990 x 624,961, 252.8M
     train / 4.0M test ratings on 0..100, k=128, 20 epochs, for fp32 / fp16 / bf16 / bf16
     with stochastic rounding / fp16 with stochastic rounding storage (fp32 arithmetic).
     Full size: throughput and test RMSE per storage type.  Gap to the serial FP64 oracle:
@@ -272,7 +272,7 @@ def run_precision_suite(args):
 
 
 def run_warmstart_suite(args, quiet=False):
-    """Learned warm start (BASELINE config 5; with --scale 2 the c2-shape headline).
+    """Learned warm start (the c1-family scenario; with --scale 2 the c2-shape headline).
 
     Scenario: a deployed model exists for a base matrix (c1 or c2 shape); 50,000 new users
     arrive with ratings amounting to 5% of the base train count (one planted model for all).
@@ -444,7 +444,7 @@ def warm_summary(args):
 
 
 def run_batched_suite(args):
-    """Batched factorizations (BASELINE config 4): 64 planted problems, users log-uniform in
+    """Batched factorizations: 64 planted problems, users log-uniform in
     [1k, 200k], items in [500, 20k], ratings in [50k, 10M], k in {32, 64, 128}, planted rank
     in [8, 32], integer ratings 1..5, fp16 factors, 20 epochs.
       sequential: per epoch, one plain update launch per problem (64 launches per epoch);

@@ -237,7 +237,7 @@ def test_hogwild_c1_rmse_within_0002_of_serial_oracle(lib, orc, cuda):
     """c1 (10k x 2k, 0.9M ratings, Zipf(1.0)) with 64 concurrent workers: the test RMSE after 20
     epochs is within 0.002 of the serial oracle running the same 64 workers' batches in
     round-robin order.  (With ~10k concurrent workers a 2,000-item matrix loses most of its
-    item updates to overwrites; that regime is measured, not asserted.)"""
+    item updates to overwrites; that regime is measured by the benchmarks, not asserted here.)"""
     tr, te = synth.generate_c1(seed=1, device="cpu")
     prob = cm.MFProblem.from_arrays(tr["u"], tr["v"], tr["r"], m=10000, n=2000)
     test = cm.MFProblem.from_arrays(te["u"], te["v"], te["r"])
