@@ -654,7 +654,14 @@ def run_text_suite(args):
     ok = bool(np.array_equal(got["u"], train["u"]) and np.array_equal(got["v"], train["v"]) and
               np.array_equal(got["r"], np.rint(train["r"]).astype(np.float32)))
     res = {}
-    for name, fn in (("device", device_parse), ("e2e", end_to_end)):
+    import ctypes as C
+    from cumf_sgd_gb300 import _lib
+    n_out = C.c_int64(0)
+
+    def end_to_end_pipelined():
+        _lib.check(_lib.load().cumf_parse_text_host(h_text.data_ptr(), length, 3, h_out.data_ptr(), n, C.byref(n_out)))
+
+    for name, fn in (("device", device_parse), ("e2e", end_to_end), ("e2e_pipelined", end_to_end_pipelined)):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
@@ -665,6 +672,8 @@ def run_text_suite(args):
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) / args.steps
         res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "wall_ms": wall * 1e3}
+    got = h_out.numpy().view(synth.NODE_DTYPE)
+    ok_pipe = bool(n_out.value == n and np.array_equal(got["u"], train["u"]) and np.array_equal(got["v"], train["v"]))
     # Oracle (strtol/strtof, one core) on a bounded prefix of the same text.
     sample_lines = min(n, 4_000_000)
     cut = int(np.searchsorted(np.cumsum(h_text[start:length].numpy() == 10), sample_lines)) + start + 1
@@ -673,9 +682,12 @@ def run_text_suite(args):
     recs = oracle.parse_text(sample)
     cpu_s = time.perf_counter() - t0
     print(json.dumps({"suite": "text", "records": n, "text_bytes": length, "parse_matches_records": ok,
+                      "pipelined_matches_records": ok_pipe,
                       "device_ms": res["device"]["ms"], "device_GBps": length / res["device"]["ms"] / 1e6,
                       "device_records_per_s": n / res["device"]["ms"] * 1e3,
                       "e2e_ms": res["e2e"]["ms"], "e2e_records_per_s": n / res["e2e"]["ms"] * 1e3,
+                      "e2e_pipelined_ms": res["e2e_pipelined"]["wall_ms"],
+                      "e2e_pipelined_records_per_s": n / res["e2e_pipelined"]["wall_ms"] * 1e3,
                       "e2e_h2d_bytes": length, "e2e_d2h_bytes": n * 12,
                       "cpu_oracle": {"records": len(recs), "seconds": cpu_s, "records_per_s": len(recs) / cpu_s,
                                      "cores": 1, "kind": "port (strtol/strtof)"}}), flush=True)

@@ -188,6 +188,18 @@ def read_text_problem(path: str, header_lines: int = 3, pinned: bool = True) -> 
     return MFProblem(c)
 
 
+def parse_text_host(text, header_lines: int = 3) -> np.ndarray:
+    """Rating text (bytes) -> records with the copies and the parse overlapped in chunks."""
+    buf = np.frombuffer(text, dtype=np.uint8) if isinstance(text, (bytes, bytearray)) else text
+    n = C.c_int64(0)
+    L = _lib.load()
+    _lib.check(L.cumf_parse_text_host(buf.ctypes.data, len(buf), header_lines, None, 0, C.byref(n)))
+    out = np.zeros(n.value, dtype=NODE_DTYPE)
+    _lib.check(L.cumf_parse_text_host(buf.ctypes.data, len(buf), header_lines, out.ctypes.data if n.value else None,
+                                      n.value, C.byref(n)))
+    return out
+
+
 def text_data_start(text: bytes, header_lines: int = 3) -> int:
     """Offset of the first data byte after the header lines (transform.cpp:31-33)."""
     out = C.c_int64(0)

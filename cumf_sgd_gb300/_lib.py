@@ -110,6 +110,7 @@ _SIGS = {
     "cumf_evaluate": (C.c_int, [C.POINTER(Problem), C.POINTER(Model), C.c_int, C.POINTER(C.c_double)]),
     "cumf_convert_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_read_text_problem": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Problem)]),
+    "cumf_parse_text_host": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "cumf_text_data_start": (C.c_int, [C.c_char_p, C.c_int64, C.c_int, C.POINTER(C.c_int64)]),
     "cumf_dev_parse_text": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
                                       C.POINTER(C.c_int64), C.c_void_p]),

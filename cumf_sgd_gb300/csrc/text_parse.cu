@@ -31,6 +31,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <vector>
 #include <string>
 
 #include "cumf_sgd.h"
@@ -391,10 +392,13 @@ __device__ uint32_t parse_float(const unsigned char *t, int64_t i, int64_t len, 
     return 0;
 }
 
+// carry: tokens before this text (chunks of a longer text; NULL = none); byte_base: the text's
+// offset in the whole input, for error positions.
 __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned char *__restrict__ t, int64_t start,
                                                            int64_t len, const unsigned long long *block_base,
                                                            uint32_t *out_words, unsigned long long cap_tokens,
-                                                           unsigned long long *bad) {
+                                                           unsigned long long *bad, const unsigned long long *carry,
+                                                           int64_t byte_base) {
     const int64_t seg = ((int64_t)blockIdx.x * kTB + threadIdx.x) * kSeg;
     uint64_t starts = start_mask(t, seg, start, len);
     const unsigned c = (unsigned)__popcll(starts);
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned cha
     __syncthreads();
     unsigned wbase = 0;
     for (int w = 0; w < warp; ++w) wbase += s_w[w];
-    unsigned long long tok = block_base[blockIdx.x] + wbase + (incl - c);
+    unsigned long long tok = block_base[blockIdx.x] + wbase + (incl - c) + (carry ? *carry : 0ull);
     while (starts) {
         const int j = __ffsll((long long)starts) - 1;
         starts &= starts - 1;
@@ -427,9 +431,14 @@ __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned cha
             word = __float_as_uint(f);
         }
         if (reason == 0 && tok < cap_tokens) out_words[tok] = word;
-        if (reason != 0) atomicMin(bad, ((unsigned long long)i << 8) | reason);
+        if (reason != 0) atomicMin(bad, ((unsigned long long)(i + byte_base) << 8) | reason);
         ++tok;
     }
+}
+
+// After a chunk: carry += the chunk's token count (counts[nb]); host_carry receives it.
+__global__ void advance_carry_kernel(unsigned long long *carry, const unsigned long long *chunk_total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *carry += *chunk_total;
 }
 
 const char *reason_text(uint32_t r) {
@@ -498,7 +507,7 @@ int parse_text_device(const unsigned char *d_text, int64_t len, int64_t start, c
         CUMF_CUDA(cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), s));
         parse_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts,
                                                          reinterpret_cast<uint32_t *>(d_out),
-                                                         (unsigned long long)cap * 3ull, bad);
+                                                         (unsigned long long)cap * 3ull, bad, nullptr, 0);
         CUMF_CUDA(cudaGetLastError());
         CUMF_CUDA(cudaMemcpyAsync(tail, counts + nb, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     } else {
@@ -514,6 +523,129 @@ int parse_text_device(const unsigned char *d_text, int64_t len, int64_t start, c
         return fail(CUMF_ERR_FORMAT, "parse_text: byte " + std::to_string(tail[1] >> 8) + ": " +
                                          reason_text((uint32_t)(tail[1] & 0xffu)));
     if (d_out && cap < *n_records)
+        return fail(CUMF_ERR_ARG, "parse_text: output holds " + std::to_string(cap) + " records, " +
+                                      std::to_string(*n_records) + " needed");
+    return CUMF_OK;
+}
+
+// Host text -> host records with the copies overlapped: chunks of about 64 MB, each
+// starting right after a whitespace byte (no token crosses a boundary), go H2D on one stream,
+// are counted, scanned and parsed on another, and the records completed so far go D2H on a
+// third while later chunks are still arriving.  Token indices continue across chunks through
+// a device carry, so a record may span two chunks.
+int parse_text_host(const unsigned char *h_text, int64_t len, int64_t start, cumf_node *h_out, int64_t cap,
+                    int64_t *n_records) {
+    constexpr int64_t kChunk = 64ll << 20;
+    *n_records = 0;
+    if (start >= len) return CUMF_OK;
+    std::vector<int64_t> bounds{start};
+    while (bounds.back() < len) {
+        int64_t b = std::min(len, bounds.back() + kChunk);
+        while (b < len && !(h_text[b - 1] == ' ' || (h_text[b - 1] >= '\t' && h_text[b - 1] <= '\r'))) ++b;
+        bounds.push_back(b);
+    }
+    const int chunks = (int)bounds.size() - 1;
+    int64_t max_chunk = 0;
+    for (int c = 0; c < chunks; ++c) max_chunk = std::max(max_chunk, bounds[c + 1] - bounds[c]);
+    const int64_t max_nb = (max_chunk + kBlockBytes - 1) / kBlockBytes;
+    const int64_t rec_cap = (len - start) / 6 + 2;  // tokens are at least 2 bytes apart
+    struct Dev {
+        void *p = nullptr;
+        ~Dev() {
+            if (p) cudaFree(p);
+        }
+    } slot[2], counts[2], recs, small;
+    struct Stm {
+        cudaStream_t s = nullptr;
+        ~Stm() {
+            if (s) cudaStreamDestroy(s);
+        }
+    } h2d, comp, d2h;
+    struct Evs {
+        std::vector<cudaEvent_t> e;
+        ~Evs() {
+            for (cudaEvent_t x : e) cudaEventDestroy(x);
+        }
+        cudaEvent_t make() {
+            cudaEvent_t x = nullptr;
+            if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess) e.push_back(x);
+            return x;
+        }
+    } evs;
+    struct PinnedCarry {
+        unsigned long long *p = nullptr;
+        ~PinnedCarry() {
+            if (p) cudaFreeHost(p);
+        }
+    } hc;
+    for (int k = 0; k < 2; ++k) {
+        CUMF_CUDA(cudaMalloc(&slot[k].p, (size_t)max_chunk + 16));
+        CUMF_CUDA(cudaMalloc(&counts[k].p, (size_t)(max_nb + 1) * sizeof(unsigned long long)));
+    }
+    CUMF_CUDA(cudaMalloc(&recs.p, (size_t)rec_cap * sizeof(cumf_node)));
+    CUMF_CUDA(cudaMalloc(&small.p, 2 * sizeof(unsigned long long)));  // carry, first bad token
+    CUMF_CUDA(cudaMallocHost(&hc.p, (size_t)(chunks + 1) * sizeof(unsigned long long)));
+    unsigned long long *carry = static_cast<unsigned long long *>(small.p), *bad = carry + 1;
+    CUMF_CUDA(cudaStreamCreateWithFlags(&h2d.s, cudaStreamNonBlocking));
+    CUMF_CUDA(cudaStreamCreateWithFlags(&comp.s, cudaStreamNonBlocking));
+    CUMF_CUDA(cudaStreamCreateWithFlags(&d2h.s, cudaStreamNonBlocking));
+    CUMF_CUDA(cudaMemsetAsync(carry, 0, sizeof(unsigned long long), comp.s));
+    CUMF_CUDA(cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), comp.s));
+    std::vector<cudaEvent_t> copied(chunks), parsed(chunks);
+    for (int c = 0; c < chunks; ++c) {
+        copied[c] = evs.make();
+        parsed[c] = evs.make();
+        if (!copied[c] || !parsed[c]) return fail(CUMF_ERR_CUDA, "parse_text_host: events");
+    }
+    int64_t sent = 0;  // records already copied back
+    uint32_t *words = static_cast<uint32_t *>(recs.p);
+    const unsigned long long cap_tokens = (unsigned long long)rec_cap * 3ull;
+    auto flush_done = [&](int c) -> int {  // copy back the records completed by chunk c
+        CUMF_CUDA(cudaEventSynchronize(parsed[c]));
+        const int64_t done = (int64_t)(hc.p[c + 1] / 3ull);
+        const int64_t upto = std::min(done, cap);
+        if (h_out && upto > sent) {
+            CUMF_CUDA(cudaMemcpyAsync(h_out + sent, static_cast<cumf_node *>(recs.p) + sent,
+                                      (size_t)(upto - sent) * sizeof(cumf_node), cudaMemcpyDeviceToHost, d2h.s));
+            sent = upto;
+        }
+        return CUMF_OK;
+    };
+    for (int c = 0; c < chunks; ++c) {
+        const int k = c & 1;
+        const int64_t clen = bounds[c + 1] - bounds[c];
+        const int64_t nb = (clen + kBlockBytes - 1) / kBlockBytes;
+        if (c >= 2) CUMF_CUDA(cudaStreamWaitEvent(h2d.s, parsed[c - 2], 0));  // the slot is free again
+        CUMF_CUDA(cudaMemcpyAsync(slot[k].p, h_text + bounds[c], (size_t)clen, cudaMemcpyHostToDevice, h2d.s));
+        CUMF_CUDA(cudaEventRecord(copied[c], h2d.s));
+        CUMF_CUDA(cudaStreamWaitEvent(comp.s, copied[c], 0));
+        const unsigned char *t = static_cast<const unsigned char *>(slot[k].p);
+        unsigned long long *cnt = static_cast<unsigned long long *>(counts[k].p);
+        count_tokens_kernel<<<(unsigned)nb, kTB, 0, comp.s>>>(t, 0, clen, cnt);
+        scan_blocks_kernel<<<1, kScanThreads, 0, comp.s>>>(cnt, nb);
+        parse_tokens_kernel<<<(unsigned)nb, kTB, 0, comp.s>>>(t, 0, clen, cnt, words, cap_tokens, bad, carry,
+                                                               bounds[c]);
+        advance_carry_kernel<<<1, 32, 0, comp.s>>>(carry, cnt + nb);
+        CUMF_CUDA(cudaGetLastError());
+        CUMF_CUDA(cudaMemcpyAsync(hc.p + c + 1, carry, sizeof(unsigned long long), cudaMemcpyDeviceToHost, comp.s));
+        CUMF_CUDA(cudaEventRecord(parsed[c], comp.s));
+        if (c >= 1)  // chunk c is queued: copy back what chunk c - 1 completed meanwhile
+            if (int rc = flush_done(c - 1)) return rc;
+    }
+    if (int rc = flush_done(chunks - 1)) return rc;
+    unsigned long long first_bad = 0;
+    CUMF_CUDA(cudaMemcpyAsync(&first_bad, bad, sizeof(first_bad), cudaMemcpyDeviceToHost, comp.s));
+    CUMF_CUDA(cudaStreamSynchronize(comp.s));
+    CUMF_CUDA(cudaStreamSynchronize(d2h.s));
+    const unsigned long long total = hc.p[chunks];
+    if (total % 3 != 0)
+        return fail(CUMF_ERR_FORMAT, "parse_text: " + std::to_string(total) +
+                                         " tokens do not form whole (u, v, r) records");
+    *n_records = (int64_t)(total / 3);
+    if (first_bad != ~0ull)
+        return fail(CUMF_ERR_FORMAT, "parse_text: byte " + std::to_string(first_bad >> 8) + ": " +
+                                         reason_text((uint32_t)(first_bad & 0xffu)));
+    if (h_out && cap < *n_records)
         return fail(CUMF_ERR_ARG, "parse_text: output holds " + std::to_string(cap) + " records, " +
                                       std::to_string(*n_records) + " needed");
     return CUMF_OK;
@@ -677,4 +809,12 @@ extern "C" int cumf_convert_text(const char *in_path, const char *out_path, int 
     cumf_free_problem(&p);
     if (rc == CUMF_OK && n_records) *n_records = n;
     return rc;
+}
+
+extern "C" int cumf_parse_text_host(const char *text, int64_t len, int header_lines, cumf_node *out, int64_t cap,
+                                    int64_t *n_records) {
+    if (!n_records || len < 0 || (len > 0 && !text) || header_lines < 0 || cap < 0 || (out == nullptr && cap > 0))
+        return fail(CUMF_ERR_ARG, "parse_text_host: bad arguments");
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(text);
+    return parse_text_host(p, len, text_data_start(p, len, header_lines), out, cap, n_records);
 }

@@ -211,6 +211,11 @@ int cumf_convert_text(const char *in_path, const char *out_path, int header_line
 int cumf_read_text_problem(const char *path, int header_lines, int pinned, cumf_problem *out);
 /* Host helper: offset of the first data byte after `header_lines` header lines. */
 int cumf_text_data_start(const char *text, int64_t len, int header_lines, int64_t *start);
+/* Host text (preferably page-locked) -> host records, the text's copy, the parse and the
+ * records' copy overlapped in chunks of about 64 MB.  Same rules as cumf_convert_text;
+ * *n_records receives the count (out may be NULL with cap 0 to count only). */
+int cumf_parse_text_host(const char *text, int64_t len, int header_lines, cumf_node *out, int64_t cap,
+                         int64_t *n_records);
 /* Device-level parse of text bytes [start, len) of d_text (16-byte aligned device memory)
  * into d_out.  *n_records receives the record count; with d_out == NULL only the count is
  * computed.  A d_out with cap < count fails with CUMF_ERR_ARG. Synchronises the stream. */

@@ -160,3 +160,17 @@ def test_valid_spellings_mid_text(lib, cuda, orc, tmp_path):
     p.write_bytes(text)
     assert cm.convert_text(str(p)) == len(toks) + 12
     assert (tmp_path / "ok.txt.bin").read_bytes() == orc.parse_text(text).tobytes()
+
+
+def test_host_pipeline_matches_oracle_across_chunks(lib, cuda, orc):
+    """More than one 64 MB chunk: records that straddle chunk boundaries, copies overlapped."""
+    import cumf_sgd_gb300 as cm
+    block = random_text(200_000, 11)
+    head_end = cm.text_data_start(block)
+    body = block[head_end:]
+    text = block[:head_end] + body * ((70 << 20) // len(body) + 1)
+    exp = orc.parse_text(text)
+    got = cm.parse_text_host(text)
+    assert len(got) == len(exp) and got.tobytes() == exp.tobytes()
+    for name, (small, ref) in fixtures().items():
+        assert cm.parse_text_host(small).tobytes() == ref, name
