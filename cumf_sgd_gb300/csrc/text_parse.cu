@@ -36,6 +36,7 @@
 
 #include "cumf_sgd.h"
 #include "internal.h"
+#include "text_token.h"
 
 namespace cumf {
 
@@ -44,12 +45,20 @@ namespace {
 constexpr int kSeg = 64;                         // bytes per thread
 constexpr int kTB = 256;                         // threads per block
 constexpr int64_t kBlockBytes = (int64_t)kSeg * kTB;
+constexpr int kStage = (int)kBlockBytes + 64;   // a block's text plus the halo staged by the parse
 constexpr int kScanThreads = 1024;
 constexpr int kMaxToken = 1024;                  // longer tokens are rejected
 
 enum : uint32_t { kBadInt = 1, kBadIntRange = 2, kBadFloat = 3, kBadDigits = 4, kBadLong = 5 };
 
 __device__ __forceinline__ bool is_space(uint32_t c) { return c == 32u || (c - 9u) <= 4u; }
+
+// Bit j: byte j of the 16 is not a space.
+__device__ __forceinline__ uint64_t nonspace16(uint4 v) {
+    const uint64_t lo = ((uint64_t)v.y << 32) | v.x, hi = ((uint64_t)v.w << 32) | v.z;
+    return (uint64_t)(~(text_token::byte_flags(text_token::space_bytes(lo)) |
+                        (text_token::byte_flags(text_token::space_bytes(hi)) << 8)) & 0xffffu);
+}
 
 // Bit j of the result: byte seg+j is inside [start, len) and is not a space.
 __device__ __forceinline__ uint64_t nonspace_mask(const unsigned char *__restrict__ t, int64_t seg, int64_t start,
@@ -58,18 +67,7 @@ __device__ __forceinline__ uint64_t nonspace_mask(const unsigned char *__restric
     if (seg + kSeg <= len) {
         const uint4 *p = reinterpret_cast<const uint4 *>(t + seg);
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            const uint4 v = __ldg(p + w);
-            const uint32_t words[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const uint32_t c = (words[k] >> (8 * b)) & 0xffu;
-                    if (!is_space(c)) ns |= 1ull << (w * 16 + k * 4 + b);
-                }
-            }
-        }
+        for (int w = 0; w < 4; ++w) ns |= nonspace16(__ldg(p + w)) << (16 * w);
     } else {
         for (int j = 0; j < kSeg && seg + j < len; ++j)
             if (!is_space(__ldg(t + seg + j))) ns |= 1ull << j;
@@ -282,7 +280,7 @@ __device__ __forceinline__ uint32_t at(const unsigned char *t, int64_t i, int64_
 }
 
 // %d: [+-]digits, within int32.  Returns 0 or a failure reason.
-__device__ uint32_t parse_int(const unsigned char *t, int64_t i, int64_t len, int32_t *out) {
+__device__ __forceinline__ uint32_t parse_int(const unsigned char *t, int64_t i, int64_t len, int32_t *out) {
     uint32_t c = at(t, i, len);
     bool neg = false;
     if (c == '+' || c == '-') {
@@ -307,7 +305,7 @@ __device__ uint32_t parse_int(const unsigned char *t, int64_t i, int64_t len, in
 __device__ __forceinline__ uint32_t lower(uint32_t c) { return (c >= 'A' && c <= 'Z') ? c + 32u : c; }
 
 // %f: [+-](digits[.digits]|.digits)([eE][+-]digits) | [+-](inf|infinity|nan).
-__device__ uint32_t parse_float(const unsigned char *t, int64_t i, int64_t len, float *out) {
+__device__ __forceinline__ uint32_t parse_float(const unsigned char *t, int64_t i, int64_t len, float *out) {
     uint32_t c = at(t, i, len);
     bool neg = false;
     if (c == '+' || c == '-') {
@@ -392,19 +390,84 @@ __device__ uint32_t parse_float(const unsigned char *t, int64_t i, int64_t len, 
     return 0;
 }
 
+// The general parse of the token at byte i: (failure reason << 32) | the field's 32 bits.
+// Out of line, so the short-token path of parse_tokens_kernel keeps few registers.
+__device__ __noinline__ uint64_t parse_general(const unsigned char *t, int64_t i, int64_t len, bool is_rating) {
+    uint32_t reason, word;
+    if (is_rating) {
+        float f = 0.f;
+        reason = parse_float(t, i, len, &f);
+        word = __float_as_uint(f);
+    } else {
+        int32_t v = 0;
+        reason = parse_int(t, i, len, &v);
+        word = (uint32_t)v;
+    }
+    return ((uint64_t)reason << 32) | word;
+}
+
 // carry: tokens before this text (chunks of a longer text; NULL = none); byte_base: the text's
 // offset in the whole input, for error positions.
-__global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned char *__restrict__ t, int64_t start,
-                                                           int64_t len, const unsigned long long *block_base,
-                                                           uint32_t *out_words, unsigned long long cap_tokens,
-                                                           unsigned long long *bad, const unsigned long long *carry,
-                                                           int64_t byte_base) {
-    const int64_t seg = ((int64_t)blockIdx.x * kTB + threadIdx.x) * kSeg;
-    uint64_t starts = start_mask(t, seg, start, len);
+//
+// The block's 16 KB of text and a 64-byte halo are staged in shared memory with coalesced
+// 16-byte loads (bytes at or past len read as spaces).  Two passes over the blocks:
+//   - kGeneral = false: every token is offered to the byte-parallel converter on the 8 bytes at
+//     its start (text_token.h) and stored when taken; block_flags[b] records whether block b
+//     holds a token it did not take.  No call, 32 registers, 8 blocks per SM.
+//   - kGeneral = true: flagged blocks only; their remaining tokens are parsed by parse_int /
+//     parse_float from global memory, and failures are reported through `bad`.
+template <bool kGeneral>
+__global__ void __launch_bounds__(kTB, kGeneral ? 4 : 8)
+parse_tokens_kernel(const unsigned char *__restrict__ t, int64_t start, int64_t len,
+                    const unsigned long long *block_base, uint32_t *out_words, unsigned long long cap_tokens,
+                    unsigned long long *bad, const unsigned long long *carry, int64_t byte_base,
+                    uint32_t *block_flags) {
+    if (kGeneral && block_flags[blockIdx.x] == 0) return;
+    __shared__ __align__(16) unsigned char s_text[kStage];
+    const int64_t blk0 = (int64_t)blockIdx.x * kBlockBytes;
+    for (int q = threadIdx.x; q < kStage / 16; q += kTB) {
+        const int64_t g = blk0 + 16 * (int64_t)q;
+        uint4 v;
+        if (g + 16 <= len) {
+            v = __ldg(reinterpret_cast<const uint4 *>(t + g));
+        } else {
+            uint32_t w[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                w[k] = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int64_t i = g + 4 * k + b;
+                    w[k] |= (i < len ? (uint32_t)__ldg(t + i) : 32u) << (8 * b);
+                }
+            }
+            v = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        *reinterpret_cast<uint4 *>(s_text + 16 * q) = v;
+    }
+    __syncthreads();
+
+    const int base = threadIdx.x * kSeg;
+    const int64_t seg = blk0 + base;
+    uint64_t starts = 0, ns = 0;  // token starts; non-space bytes of [start, len)
+    if (seg < len && seg + kSeg > start) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(s_text + base);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) ns |= nonspace16(p[w]) << (16 * w);
+        if (start > seg) ns &= (start - seg >= kSeg) ? 0ull : (~0ull << (start - seg));
+        const uint32_t before = base > 0 ? (uint32_t)s_text[base - 1] : (seg > 0 ? (uint32_t)__ldg(t + seg - 1) : 32u);
+        const uint64_t prev = (seg - 1 >= start && !is_space(before)) ? 1ull : 0ull;
+        starts = ns & ~((ns << 1) | prev);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // Non-space bytes of the next segment (its first 16 bytes are enough for tokens of up to 7
+    // characters): the next lane's mask, or for the last lane the staged bytes after its own
+    // (base + 80 <= kStage).  Bytes there before `start` cannot follow a token of this segment.
+    uint64_t ns_next = __shfl_down_sync(0xffffffffu, ns, 1);
+    if (lane == 31) ns_next = nonspace16(*reinterpret_cast<const uint4 *>(s_text + base + kSeg));
     const unsigned c = (unsigned)__popcll(starts);
     // Block-wide exclusive scan of the per-thread counts.
     unsigned incl = c;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned x = __shfl_up_sync(0xffffffffu, incl, o);
@@ -416,24 +479,49 @@ __global__ void __launch_bounds__(kTB, 4) parse_tokens_kernel(const unsigned cha
     unsigned wbase = 0;
     for (int w = 0; w < warp; ++w) wbase += s_w[w];
     unsigned long long tok = block_base[blockIdx.x] + wbase + (incl - c) + (carry ? *carry : 0ull);
+    int field = (int)(tok % 3ull);
+    bool left = false;  // a token the byte-parallel converter did not take
+    const uint32_t *s32 = reinterpret_cast<const uint32_t *>(s_text);
     while (starts) {
         const int j = __ffsll((long long)starts) - 1;
         starts &= starts - 1;
-        const int64_t i = seg + j;
-        uint32_t reason = 0, word = 0;
-        if (tok % 3ull < 2) {
-            int32_t v = 0;
-            reason = parse_int(t, i, len, &v);
-            word = (uint32_t)v;
-        } else {
-            float f = 0.f;
-            reason = parse_float(t, i, len, &f);
-            word = __float_as_uint(f);
+        // The 8 bytes at the token's start (p + 12 <= kStage: p < kBlockBytes).
+        const int p = base + j;
+        const uint32_t a = s32[p >> 2], b = s32[(p >> 2) + 1], c2 = s32[(p >> 2) + 2];
+        const int sh = (p & 3) * 8;
+        const uint64_t x = ((uint64_t)__funnelshift_r(b, c2, sh) << 32) | __funnelshift_r(a, b, sh);
+        // Token length: the first space in the 8 bytes (none: 8 or more characters).
+        const uint32_t after = (uint32_t)(j ? (ns >> j) | (ns_next << (64 - j)) : ns);
+        const uint32_t spaces = ~after & 0xffu;
+        uint32_t word = 0;
+        const bool taken = spaces != 0 && text_token::convert_n(x, __ffs(spaces) - 1, field == 2, &word);
+        if (!kGeneral) {
+            if (taken && tok < cap_tokens) out_words[tok] = word;
+            left |= !taken;
+        } else if (!taken) {
+            const int64_t i = seg + j;
+            const uint64_t r = parse_general(t, i, len, field == 2);
+            const uint32_t reason = (uint32_t)(r >> 32);
+            if (reason == 0 && tok < cap_tokens) out_words[tok] = (uint32_t)r;
+            if (reason != 0) atomicMin(bad, ((unsigned long long)(i + byte_base) << 8) | reason);
         }
-        if (reason == 0 && tok < cap_tokens) out_words[tok] = word;
-        if (reason != 0) atomicMin(bad, ((unsigned long long)(i + byte_base) << 8) | reason);
         ++tok;
+        field = field == 2 ? 0 : field + 1;
     }
+    if (!kGeneral) {
+        const int any = __syncthreads_or(left ? 1 : 0);
+        if (threadIdx.x == 0) block_flags[blockIdx.x] = (uint32_t)any;
+    }
+}
+
+// Both passes of the parse over nb blocks of 16 KB.
+void launch_parse(const unsigned char *t, int64_t start, int64_t len, int64_t nb, const unsigned long long *block_base,
+                  uint32_t *out_words, unsigned long long cap_tokens, unsigned long long *bad,
+                  const unsigned long long *carry, int64_t byte_base, uint32_t *block_flags, cudaStream_t s) {
+    parse_tokens_kernel<false><<<(unsigned)nb, kTB, 0, s>>>(t, start, len, block_base, out_words, cap_tokens, bad,
+                                                            carry, byte_base, block_flags);
+    parse_tokens_kernel<true><<<(unsigned)nb, kTB, 0, s>>>(t, start, len, block_base, out_words, cap_tokens, bad,
+                                                           carry, byte_base, block_flags);
 }
 
 // After a chunk: carry += the chunk's token count (counts[nb]); host_carry receives it.
@@ -493,11 +581,13 @@ int parse_text_device(const unsigned char *d_text, int64_t len, int64_t start, c
     if (start >= len) return CUMF_OK;
     const int64_t nb = (len + kBlockBytes - 1) / kBlockBytes;
     if (nb > 0x7fffffffll) return fail(CUMF_ERR_ARG, "parse_text: text too large");
-    // Stream-ordered scratch: block counts, then the total, then the first-bad word.
+    // Stream-ordered scratch: block counts, then the total, then the first-bad word, then the
+    // block flags of the parse.
     StreamBuf scratch(s);
-    CUMF_CUDA(cudaMallocAsync(&scratch.p, (size_t)(nb + 2) * sizeof(unsigned long long), s));
+    CUMF_CUDA(cudaMallocAsync(&scratch.p, (size_t)(nb + 2) * sizeof(unsigned long long) + (size_t)nb * 4, s));
     unsigned long long *counts = static_cast<unsigned long long *>(scratch.p);
     unsigned long long *bad = counts + nb + 1;
+    uint32_t *flags = reinterpret_cast<uint32_t *>(counts + nb + 2);
     count_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts);
     scan_blocks_kernel<<<1, kScanThreads, 0, s>>>(counts, nb);
     CUMF_CUDA(cudaGetLastError());
@@ -505,9 +595,8 @@ int parse_text_device(const unsigned char *d_text, int64_t len, int64_t start, c
     if (d_out) {
         // Parse in the same pass; records past `cap` are parsed (for errors) but not stored.
         CUMF_CUDA(cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), s));
-        parse_tokens_kernel<<<(unsigned)nb, kTB, 0, s>>>(d_text, start, len, counts,
-                                                         reinterpret_cast<uint32_t *>(d_out),
-                                                         (unsigned long long)cap * 3ull, bad, nullptr, 0);
+        launch_parse(d_text, start, len, nb, counts, reinterpret_cast<uint32_t *>(d_out), (unsigned long long)cap * 3ull,
+                     bad, nullptr, 0, flags, s);
         CUMF_CUDA(cudaGetLastError());
         CUMF_CUDA(cudaMemcpyAsync(tail, counts + nb, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     } else {
@@ -580,7 +669,8 @@ int parse_text_host(const unsigned char *h_text, int64_t len, int64_t start, cum
     } hc;
     for (int k = 0; k < 2; ++k) {
         CUMF_CUDA(cudaMalloc(&slot[k].p, (size_t)max_chunk + 16));
-        CUMF_CUDA(cudaMalloc(&counts[k].p, (size_t)(max_nb + 1) * sizeof(unsigned long long)));
+        // block counts and the total, then the parse's block flags
+        CUMF_CUDA(cudaMalloc(&counts[k].p, (size_t)(max_nb + 1) * sizeof(unsigned long long) + (size_t)max_nb * 4));
     }
     CUMF_CUDA(cudaMalloc(&recs.p, (size_t)rec_cap * sizeof(cumf_node)));
     CUMF_CUDA(cudaMalloc(&small.p, 2 * sizeof(unsigned long long)));  // carry, first bad token
@@ -623,8 +713,8 @@ int parse_text_host(const unsigned char *h_text, int64_t len, int64_t start, cum
         unsigned long long *cnt = static_cast<unsigned long long *>(counts[k].p);
         count_tokens_kernel<<<(unsigned)nb, kTB, 0, comp.s>>>(t, 0, clen, cnt);
         scan_blocks_kernel<<<1, kScanThreads, 0, comp.s>>>(cnt, nb);
-        parse_tokens_kernel<<<(unsigned)nb, kTB, 0, comp.s>>>(t, 0, clen, cnt, words, cap_tokens, bad, carry,
-                                                               bounds[c]);
+        launch_parse(t, 0, clen, nb, cnt, words, cap_tokens, bad, carry, bounds[c],
+                     reinterpret_cast<uint32_t *>(cnt + max_nb + 1), comp.s);
         advance_carry_kernel<<<1, 32, 0, comp.s>>>(carry, cnt + nb);
         CUMF_CUDA(cudaGetLastError());
         CUMF_CUDA(cudaMemcpyAsync(hc.p + c + 1, carry, sizeof(unsigned long long), cudaMemcpyDeviceToHost, comp.s));

@@ -174,3 +174,62 @@ def test_host_pipeline_matches_oracle_across_chunks(lib, cuda, orc):
     assert len(got) == len(exp) and got.tobytes() == exp.tobytes()
     for name, (small, ref) in fixtures().items():
         assert cm.parse_text_host(small).tobytes() == ref, name
+
+
+EDGE_IDS = [b"0", b"7", b"007", b"123456", b"1234567", b"12345678", b"2147483647", b"0000000000012", b"+5"]
+EDGE_RATINGS = [b"4", b"3.5", b".5", b"5.", b"0", b"0.0", b"007.25", b"1234567", b"12345.6", b"9999999",
+                b"0.000001", b"1e3", b"+2", b"-1.5", b"inf", b"1.23456789", b"3.14159", b"0.1", b".000001",
+                b"16777217", b"9.99999", b"-0", b"2.5E+1"]
+
+
+def edge_text(n, seed, tail_newline=True):
+    """Records of edge spellings with ragged separators, so that tokens of every length start
+    at every offset of the 64-byte segments and of the 16 KB blocks (and in the halo)."""
+    rng = np.random.default_rng(seed)
+    seps = [b" ", b"\t", b"  ", b"\x0b", b"\x0c", b" \r"]
+    out = [b"h1\nh2\nh3\n"]
+    for i in range(n):
+        u = EDGE_IDS[rng.integers(len(EDGE_IDS))]
+        v = EDGE_IDS[rng.integers(len(EDGE_IDS))]
+        r = EDGE_RATINGS[rng.integers(len(EDGE_RATINGS))]
+        pad = b" " * int(rng.integers(0, 3))
+        out.append(pad + u + seps[rng.integers(len(seps))] + v + seps[rng.integers(len(seps))] + r + b"\n")
+    text = b"".join(out)
+    return text if tail_newline else text.rstrip(b"\n")
+
+
+@pytest.mark.parametrize("n,seed,tail", [(40_000, 21, True), (40_000, 22, False), (3, 23, False), (1500, 24, True)])
+def test_edge_spellings_match_oracle(lib, cuda, orc, n, seed, tail):
+    """Short tokens (byte-parallel path) and long, signed or exponent tokens (general path)
+    mixed, across segment, block and halo boundaries; text ending with and without a newline."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    text = edge_text(n, seed, tail)
+    exp = orc.parse_text(text)
+    assert len(exp) == n
+    start = cm.text_data_start(text)
+    d = torch.frombuffer(bytearray(text + b"\0" * 16), dtype=torch.uint8).to(cuda)
+    out = torch.empty(n * 12, dtype=torch.uint8, device=cuda)
+    assert cm.dev_parse_text(d.data_ptr(), len(text), start, out.data_ptr(), n) == n
+    assert out.cpu().numpy().tobytes() == exp.tobytes()
+    assert cm.parse_text_host(text).tobytes() == exp.tobytes()
+
+
+@pytest.mark.parametrize("bad", [b"4\x01", b"4\x80", b"\x7f", b"4..5", b"3.5.", b"..", b"1\x1f2", b"9\xff"])
+@pytest.mark.parametrize("where", [0, 1, 2])
+def test_short_malformed_tokens_at_the_oracle_offset(lib, cuda, orc, tmp_path, bad, where):
+    """Short tokens with control, high or repeated '.' bytes are refused by the byte-parallel
+    path and rejected by the general parser at the oracle's offset (field `where`)."""
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import _lib
+    fields = [b"11", b"22", b"3.5"]
+    fields[where] = bad
+    text = b"a\nb\nc\n" + b"7 8 9\n" * 5000 + b" ".join(fields) + b"\n" + b"7 8 9\n" * 5
+    exp = orc.parse_text(text)
+    assert exp[0] == "bad"
+    p = tmp_path / "bad.txt"
+    p.write_bytes(text)
+    with pytest.raises(cm.CumfError) as e:
+        cm.convert_text(str(p))
+    assert e.value.code == _lib.CUMF_ERR_FORMAT
+    assert "byte %d:" % exp[1] in str(e.value)
