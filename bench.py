@@ -587,6 +587,36 @@ def run_gemm_suite(args):
                           "peak_tflops": peak, "frac": tf / peak, "max_abs_err_vs_fp32": err}), flush=True)
 
 
+def run_mlp_suite(args):
+    """Warm-start MLP training (131 -> 512 -> 512 -> 128, batch 4096, Adam) on c2-sized
+    (features, factor row) pairs: time per epoch and per step (CUDA events) and the tensor-core
+    rate of the step's matrix products."""
+    import torch
+    import cumf_sgd_gb300 as cm
+    dev = torch.device("cuda", 0)
+    rows = int(3841512 * args.scale)
+    d_in, h, d_out, batch = 131, 512, 128, 4096
+    g = torch.Generator(device=dev).manual_seed(5)
+    X = torch.randn(rows, d_in, device=dev, generator=g)
+    A = torch.randn(d_in, d_out, device=dev, generator=g) / d_in ** 0.5
+    T = torch.tanh(X @ A).contiguous()
+    mlp = cm.MLP(d_in, h, d_out, seed=7)
+    mlp.train(X.data_ptr(), T.data_ptr(), min(rows, 8 * batch), epochs=1, batch=batch, seed=1)  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    loss = mlp.train(X.data_ptr(), T.data_ptr(), rows, epochs=args.mlp_epochs, batch=batch, seed=3)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    steps = args.mlp_epochs * ((rows + batch - 1) // batch)
+    dp = 192  # d_in padded to the 64-column tiles
+    flops_step = 3 * 2.0 * batch * (dp * h + h * h + h * d_out)  # forward + two backward products
+    print(json.dumps({"suite": "mlp", "rows": rows, "epochs": args.mlp_epochs, "batch": batch, "steps": steps,
+                      "train_s": ms / 1e3, "ms_per_step": ms / steps, "rows_per_s": rows * args.mlp_epochs / (ms / 1e3),
+                      "gemm_tflops_per_step": flops_step / (ms / steps * 1e-3) / 1e12, "final_loss": loss}), flush=True)
+
+
 def ratings_text_gpu(train, header: bytes):
     """The records as rating text ("u v r" lines, integer ratings), built on the GPU: digits in
     fixed-width rows, then the padding bytes dropped with one masked select."""
@@ -760,7 +790,7 @@ def main():
     ap.add_argument("--warm-configs",
                     default="bf16sr:0.04:0.3:4,bf16sr:0.02:0.05:8,bf16sr:0.04:0.3:2,fp16:0.04:0.3:4,bf16sr:0.02:0.3:0",
                     help="warm-start refinements as storage:alpha:beta:new_user_epochs, comma separated")
-    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm", "text",
+    ap.add_argument("--suite", default="", choices=["", "precision", "warmstart", "batched", "gemm", "text", "mlp",
                                                     "streamed"],
                     help="extra measurement suites (JSON lines, not the contract line)")
     args = ap.parse_args()
@@ -775,6 +805,9 @@ def main():
         return
     if args.suite == "gemm":
         run_gemm_suite(args)
+        return
+    if args.suite == "mlp":
+        run_mlp_suite(args)
         return
     if args.suite == "text":
         run_text_suite(args)

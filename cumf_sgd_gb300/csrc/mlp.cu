@@ -94,30 +94,85 @@ __global__ void user_scalar_kernel(int32_t m, int k, const float *deg, const flo
 
 // ---- elementwise helpers ---------------------------------------------------------------
 
-// rows x cols fp32 (row stride lds) -> rows x ldd bf16, zero padding for cols..ldd.
-__global__ void to_bf16_pad_kernel(const float *S, int64_t rows, int cols, int lds, __nv_bfloat16 *D, int ldd) {
-    const int64_t total = rows * ldd;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / ldd;
-        const int c = (int)(i - r * ldd);
-        D[i] = __float2bfloat16_rn(c < cols ? S[r * lds + c] : 0.f);
+// ---- 32 x 32 tile kernels: an elementwise result written row-major and transposed --------
+//
+// The weight-gradient products dW = dZ^T A take both operands K-major (K = the batch rows), so
+// every bf16 activation or gradient that feeds one is also needed transposed.  The kernels
+// below produce both copies from one read of their inputs: a block computes a 32 x 32 tile,
+// writes it row-major, stages it in shared memory (fp32, conflict-free) and writes the
+// transpose; gradient tiles also leave their 32-row column sums for the bias gradient.
+constexpr int kTile = 32;
+constexpr int kTileRows = 8;  // threads per column of a tile (blockDim = 32 x 8)
+
+// Dt[c][r] = tile[r - r0][c - c0] for the tile's valid rows r < nr and columns c < nc.
+__device__ __forceinline__ void store_tile_t(const float (*tile)[kTile + 1], __nv_bfloat16 *Dt, int64_t ldt, int r0,
+                                             int c0, int nr, int nc) {
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int c = c0 + j, r = r0 + threadIdx.x;
+        if (c < nc && r < nr) Dt[(int64_t)c * ldt + r] = __float2bfloat16_rn(tile[threadIdx.x][j]);
     }
 }
 
-// D[c][r] = S[r][c] for a rows x cols bf16 matrix (tiled through shared memory).
-// Row tiles run along gridDim.x (up to 2^31 - 1), column tiles along gridDim.y.
-__global__ void transpose_bf16_kernel(const __nv_bfloat16 *S, int rows, int cols, __nv_bfloat16 *D) {
-    __shared__ __nv_bfloat16 tile[32][33];
-    const int bx = blockIdx.y * 32, by = blockIdx.x * 32;
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const int r = by + j, c = bx + threadIdx.x;
-        tile[j][threadIdx.x] = (r < rows && c < cols) ? S[(int64_t)r * cols + c] : __float2bfloat16_rn(0.f);
+// partial[tile row][c] = the tile's column c summed over its 32 rows: each thread's own rows
+// (y, y + 8, y + 16, y + 24, in order, in `mine`), then the 8 thread sums in order.  Call after
+// a barrier that follows the writes of lanes[][] (lanes[threadIdx.y][threadIdx.x] = mine).
+__device__ __forceinline__ void tile_colsum(const float (*lanes)[kTile + 1], float *partial, int cols, int c0) {
+    if (threadIdx.y == 0 && c0 + (int)threadIdx.x < cols) {
+        float sum = 0.f;
+        for (int y = 0; y < kTileRows; ++y) sum += lanes[y][threadIdx.x];
+        partial[(int64_t)blockIdx.x * cols + c0 + threadIdx.x] = sum;
+    }
+}
+
+// D (rp x ldd bf16) and, when Dt != NULL, Dt (ldd x rp) from the fp32 rows of S (cols wide):
+// row r < valid is S[perm[*batch_idx * batch + r]] (perm NULL: S[r]); other rows and the
+// columns cols..ldd are zero.
+struct ConvertJob {
+    const float *S;
+    int cols;
+    const int32_t *perm;
+    const int *batch_idx;
+    int64_t batch;
+    int valid, rp, ldd;
+    __nv_bfloat16 *D, *Dt;
+};
+struct ConvertJobs {
+    ConvertJob job[3];  // blockIdx.z picks one; tiles outside its rp x ldd return
+};
+
+__global__ void __launch_bounds__(kTile * kTileRows) convert_t_kernel(const __grid_constant__ ConvertJobs jobs) {
+    const ConvertJob &jb = jobs.job[blockIdx.z];
+    const float *S = jb.S;
+    const int cols = jb.cols, valid = jb.valid, rp = jb.rp, ldd = jb.ldd;
+    __nv_bfloat16 *D = jb.D, *Dt = jb.Dt;
+    __shared__ float tile[kTile][kTile + 1];
+    const int r0 = blockIdx.x * kTile, c0 = blockIdx.y * kTile;
+    if (r0 >= rp || c0 >= ldd) return;
+    const int32_t *idx = jb.perm ? jb.perm + (int64_t)*jb.batch_idx * jb.batch : nullptr;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
+        float v = 0.f;
+        if (r < valid && c < cols) v = S[(int64_t)(idx ? idx[r] : r) * cols + c];
+        const __nv_bfloat16 b = __float2bfloat16_rn(v);
+        if (r < rp && c < ldd) D[(int64_t)r * ldd + c] = b;
+        tile[j][threadIdx.x] = __bfloat162float(b);
+    }
+    if (!Dt) return;
+    __syncthreads();
+    store_tile_t(tile, Dt, rp, r0, c0, rp, ldd);
+}
+
+// D^T (cols x rows) of a bf16 matrix D (rows x cols).
+__global__ void __launch_bounds__(kTile * kTileRows) transpose_t_kernel(const __nv_bfloat16 *D, int rows, int cols,
+                                                                        __nv_bfloat16 *Dt) {
+    __shared__ float tile[kTile][kTile + 1];
+    const int r0 = blockIdx.x * kTile, c0 = blockIdx.y * kTile;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
+        tile[j][threadIdx.x] = (r < rows && c < cols) ? __bfloat162float(D[(int64_t)r * cols + c]) : 0.f;
     }
     __syncthreads();
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const int c = bx + j, r = by + threadIdx.x;
-        if (c < cols && r < rows) D[(int64_t)c * rows + r] = tile[threadIdx.x][j];
-    }
+    store_tile_t(tile, Dt, rows, r0, c0, rows, cols);
 }
 
 __device__ __forceinline__ float gelu_grad(float x) {
@@ -127,46 +182,111 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * c * (1.f + 3.f * 0.044715f * x * x);
 }
 
-// dZ = dA * gelu'(pre) -> bf16; rows beyond `valid` are zero.
-__global__ void gelu_back_kernel(const float *dA, const float *pre, int64_t rows, int64_t valid, int cols,
-                                 __nv_bfloat16 *dZ) {
-    const int64_t total = rows * cols;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / cols;
-        dZ[i] = __float2bfloat16_rn(r < valid ? dA[i] * gelu_grad(pre[i]) : 0.f);
+// dZ = dA * gelu'(pre) -> bf16 (rows beyond `valid` zero), its transpose dZt, and the tile
+// column sums of dZ (the bias gradient's partial sums).
+__global__ void __launch_bounds__(kTile * kTileRows) gelu_back_t_kernel(const float *dA, const float *pre, int rp,
+                                                                        int valid, int cols, __nv_bfloat16 *dZ,
+                                                                        __nv_bfloat16 *dZt, float *partial) {
+    __shared__ float tile[kTile][kTile + 1];
+    __shared__ float lanes[kTileRows][kTile + 1];
+    const int r0 = blockIdx.x * kTile, c0 = blockIdx.y * kTile;
+    float mine = 0.f;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
+        const int64_t i = (int64_t)r * cols + c;
+        const float g = (r < valid && c < cols) ? dA[i] * gelu_grad(pre[i]) : 0.f;
+        const __nv_bfloat16 b = __float2bfloat16_rn(g);
+        if (r < rp && c < cols) dZ[i] = b;
+        const float bv = __bfloat162float(b);
+        tile[j][threadIdx.x] = bv;
+        mine += bv;
     }
+    lanes[threadIdx.y][threadIdx.x] = mine;
+    __syncthreads();
+    tile_colsum(lanes, partial, cols, c0);
+    store_tile_t(tile, dZt, rp, r0, c0, rp, cols);
 }
 
-// dY = 2 (Y - T) / B (bf16, zero for padding rows) and the loss partial sums.
-__global__ void mse_grad_kernel(const float *Y, const float *T, int64_t rows, int64_t valid, int cols, float inv_b,
-                                __nv_bfloat16 *dY, double *loss) {
+// dY = 2 (Y - T) / B (bf16, zero for padding rows), its transpose, the tile column sums and
+// the loss (sum of squared errors).  Row r < valid of T is T[perm[*batch_idx * batch + r]]
+// (perm NULL: T[r]).
+__global__ void __launch_bounds__(kTile * kTileRows) mse_grad_t_kernel(const float *Y, const float *T,
+                                                                       const int32_t *perm, const int *batch_idx,
+                                                                       int64_t batch, int rp, int valid, int cols,
+                                                                       float inv_b, __nv_bfloat16 *dY,
+                                                                       __nv_bfloat16 *dYt, float *partial,
+                                                                       double *loss) {
+    __shared__ float tile[kTile][kTile + 1];
+    __shared__ float lanes[kTileRows][kTile + 1];
+    __shared__ double s_loss[kTileRows];
+    const int r0 = blockIdx.x * kTile, c0 = blockIdx.y * kTile;
+    const int32_t *idx = perm ? perm + (int64_t)*batch_idx * batch : nullptr;
     double acc = 0;
-    const int64_t total = rows * cols;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / cols;
+    float mine = 0.f;
+    for (int j = threadIdx.y; j < kTile; j += kTileRows) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
         float g = 0.f;
-        if (r < valid) {
-            const float d = Y[i] - T[i];
+        if (r < valid && c < cols) {
+            const float d = Y[(int64_t)r * cols + c] - T[(int64_t)(idx ? idx[r] : r) * cols + c];
             acc += (double)d * d;
             g = 2.f * d * inv_b;
         }
-        dY[i] = __float2bfloat16_rn(g);
+        const __nv_bfloat16 b = __float2bfloat16_rn(g);
+        if (r < rp && c < cols) dY[(int64_t)r * cols + c] = b;
+        const float bv = __bfloat162float(b);
+        tile[j][threadIdx.x] = bv;
+        mine += bv;
     }
+    lanes[threadIdx.y][threadIdx.x] = mine;
     for (int o = 16; o >= 1; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, acc);
+    if (threadIdx.x == 0) s_loss[threadIdx.y] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && loss) {
+        double t = 0;
+        for (int w = 0; w < kTileRows; ++w) t += s_loss[w];
+        atomicAdd(loss, t);
+    }
+    tile_colsum(lanes, partial, cols, c0);
+    store_tile_t(tile, dYt, rp, r0, c0, rp, cols);
 }
 
-// bias gradient: column sums of a rows x cols bf16 matrix.
-__global__ void colsum_kernel(const __nv_bfloat16 *Z, int64_t rows, int cols, float *out) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cols) return;
-    float s = 0.f;
-    for (int64_t r = 0; r < rows; ++r) s += __bfloat162float(Z[r * cols + c]);
-    out[c] = s;
+// Bias gradient: out[c] = the tile column sums of column c (tile_colsum).  Block: 32 columns x
+// 8 lanes; lane y adds tiles y, y + 8, ... in order, then the 8 lane sums are added in order.
+__global__ void __launch_bounds__(kTile * kTileRows) colsum_finish_kernel(const float *partial, int tiles, int cols,
+                                                                          float *out) {
+    __shared__ float lanes[kTileRows][kTile + 1];
+    const int c = blockIdx.x * kTile + threadIdx.x;
+    float sum = 0.f;
+    if (c < cols)
+        for (int t = threadIdx.y; t < tiles; t += kTileRows) sum += partial[(int64_t)t * cols + c];
+    lanes[threadIdx.y][threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < cols) {
+        float total = 0.f;
+        for (int y = 0; y < kTileRows; ++y) total += lanes[y][threadIdx.x];
+        out[c] = total;
+    }
 }
 
+// After a step: the next batch of the permutation, Adam's step count, the step's loss added to
+// the epoch's.  One thread; this state lives on the device so that a captured step can replay.
+__global__ void step_end_kernel(int64_t *step, int *batch_idx, const double *loss, double *loss_sum) {
+    ++*step;
+    ++*batch_idx;
+    *loss_sum += *loss;
+}
+
+// Adam step number *step + 1 (bias corrections 1 - b^t computed once per block).
 __global__ void adam_kernel(float *w, const float *g, float *m1, float *m2, int64_t n, float lr, float b1, float b2,
-                            float eps, float c1, float c2) {
+                            float eps, const int64_t *step) {
+    __shared__ float corr[2];
+    if (threadIdx.x == 0) {
+        const float t = (float)(*step + 1);
+        corr[0] = 1.f - powf(b1, t);
+        corr[1] = 1.f - powf(b2, t);
+    }
+    __syncthreads();
+    const float c1 = corr[0], c2 = corr[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float gi = g[i];
         const float a = b1 * m1[i] + (1.f - b1) * gi;
@@ -182,14 +302,6 @@ __global__ void init_weights_kernel(float *w, int64_t n, float scale, uint64_t k
         // uniform(-scale, scale) from the counter hash
         const float u = init_uniform(key, (uint64_t)i);  // (0, 1]
         w[i] = (2.f * u - 1.f) * scale;
-    }
-}
-
-__global__ void gather_rows_kernel(const float *S, int ld, const int32_t *idx, int64_t rows, float *D) {
-    const int64_t total = rows * ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / ld;
-        D[i] = S[(int64_t)idx[r] * ld + (i - r * ld)];
     }
 }
 
@@ -209,6 +321,7 @@ struct Mlp {
     int64_t cap = 0;
     DevBuf xb, h1, h2, pre1, pre2, y, dy, dyt, h2t, h1t, xbt, dh2, dp2, dp2t, dh1, dp1, dp1t, loss;
     DevBuf gw1p;  // gradient of W1 in padded layout [h][dp]
+    DevBuf colws; // (cap / 32) x max(h, d_out) tile column sums
 };
 
 namespace {
@@ -235,15 +348,44 @@ int mlp_ensure(Mlp *mp, int64_t rows) {
     CUMF_CUDA(mp->dh1.alloc(r * h * 4));
     CUMF_CUDA(mp->dp1.alloc(r * h * b2));
     CUMF_CUDA(mp->dp1t.alloc(r * h * b2));
+    CUMF_CUDA(mp->colws.alloc((r / kTile) * (h > dout ? h : dout) * 4));
     mp->cap = r;
     return CUMF_OK;
 }
 
-cudaError_t transpose(const void *S, int rows, int cols, void *D, cudaStream_t s) {
-    dim3 grid((rows + 31) / 32, (cols + 31) / 32), block(32, 8);
-    if (grid.y > 65535) return cudaErrorInvalidValue;
-    transpose_bf16_kernel<<<grid, block, 0, s>>>(reinterpret_cast<const __nv_bfloat16 *>(S), rows, cols,
-                                                  reinterpret_cast<__nv_bfloat16 *>(D));
+const dim3 kTileBlock(kTile, kTileRows);
+
+dim3 tiles_of(int64_t rows, int cols) { return dim3((unsigned)((rows + kTile - 1) / kTile), (unsigned)((cols + kTile - 1) / kTile)); }
+
+ConvertJob convert_job(const float *S, int cols, const int32_t *perm, const int *batch_idx, int64_t batch, int valid,
+                       int rp, int ldd, void *D, void *Dt) {
+    return ConvertJob{S, cols, perm, batch_idx, batch, valid, rp, ldd, static_cast<__nv_bfloat16 *>(D),
+                      static_cast<__nv_bfloat16 *>(Dt)};
+}
+
+// n (1..3) conversions in one launch.
+cudaError_t convert(const ConvertJob *job, int n, cudaStream_t s) {
+    ConvertJobs jobs{};
+    unsigned gx = 1, gy = 1;
+    for (int i = 0; i < n; ++i) {
+        jobs.job[i] = job[i];
+        const dim3 g = tiles_of(job[i].rp, job[i].ldd);
+        gx = g.x > gx ? g.x : gx;
+        gy = g.y > gy ? g.y : gy;
+    }
+    convert_t_kernel<<<dim3(gx, gy, n), kTileBlock, 0, s>>>(jobs);
+    return cudaGetLastError();
+}
+
+cudaError_t transpose(const void *D, int rows, int cols, void *Dt, cudaStream_t s) {
+    transpose_t_kernel<<<tiles_of(rows, cols), kTileBlock, 0, s>>>(static_cast<const __nv_bfloat16 *>(D), rows, cols,
+                                                                   static_cast<__nv_bfloat16 *>(Dt));
+    return cudaGetLastError();
+}
+
+cudaError_t colsum_finish(Mlp *mp, int64_t rp, int cols, float *out, cudaStream_t s) {
+    colsum_finish_kernel<<<(cols + kTile - 1) / kTile, kTileBlock, 0, s>>>(mp->colws.as<float>(), (int)(rp / kTile),
+                                                                            cols, out);
     return cudaGetLastError();
 }
 
@@ -251,27 +393,25 @@ cudaError_t transpose(const void *S, int rows, int cols, void *D, cudaStream_t s
 int mlp_refresh(Mlp *mp, cudaStream_t s) {
     const float *P = mp->params.as<float>();
     const int h = mp->h, dout = mp->d_out;
-    to_bf16_pad_kernel<<<grid_of((int64_t)h * mp->dp), kT, 0, s>>>(P + mp->off_w1, h, mp->d_in, mp->d_in,
-                                                                     mp->w1b.as<__nv_bfloat16>(), mp->dp);
-    to_bf16_pad_kernel<<<grid_of((int64_t)h * h), kT, 0, s>>>(P + mp->off_w2, h, h, h, mp->w2b.as<__nv_bfloat16>(), h);
-    to_bf16_pad_kernel<<<grid_of((int64_t)dout * h), kT, 0, s>>>(P + mp->off_w3, dout, h, h,
-                                                                   mp->w3b.as<__nv_bfloat16>(), h);
-    CUMF_CUDA(cudaGetLastError());
-    CUMF_CUDA(transpose(mp->w2b.p, h, h, mp->w2t.p, s));
-    CUMF_CUDA(transpose(mp->w3b.p, dout, h, mp->w3t.p, s));
+    const ConvertJob jobs[3] = {
+        convert_job(P + mp->off_w1, mp->d_in, nullptr, nullptr, 0, h, h, mp->dp, mp->w1b.p, nullptr),
+        convert_job(P + mp->off_w2, h, nullptr, nullptr, 0, h, h, h, mp->w2b.p, mp->w2t.p),
+        convert_job(P + mp->off_w3, h, nullptr, nullptr, 0, dout, dout, h, mp->w3b.p, mp->w3t.p)};
+    CUMF_CUDA(convert(jobs, 3, s));
     return CUMF_OK;
 }
 
-// Forward over rows [0, rows) of X (fp32, rows x d_in); Y (fp32 rows x d_out) in mp->y.
-int mlp_forward_ws(Mlp *mp, const float *X, int64_t rows, cudaStream_t s) {
+// Forward over rows [0, rows) of X (fp32, rows x d_in; with perm, row r is X[perm[*batch_idx *
+// batch + r]]); Y (fp32 rows x d_out) in mp->y.  Also leaves X's bf16 transpose for backward.
+int mlp_forward_ws(Mlp *mp, const float *X, int64_t rows, cudaStream_t s, const int32_t *perm = nullptr,
+                   const int *batch_idx = nullptr, int64_t batch = 0) {
     if (int rc = mlp_ensure(mp, rows)) return rc;
     const float *P = mp->params.as<float>();
     const int h = mp->h;
     const int64_t rp = (rows + 127) / 128 * 128;  // padding rows are zero
-    CUMF_CUDA(cudaMemsetAsync(mp->xb.p, 0, rp * mp->dp * 2, s));
-    to_bf16_pad_kernel<<<grid_of(rows * mp->dp), kT, 0, s>>>(X, rows, mp->d_in, mp->d_in, mp->xb.as<__nv_bfloat16>(),
-                                                               mp->dp);
-    CUMF_CUDA(cudaGetLastError());
+    const ConvertJob job = convert_job(X, mp->d_in, perm, batch_idx, batch, (int)rows, (int)rp, mp->dp, mp->xb.p,
+                                       mp->xbt.p);
+    CUMF_CUDA(convert(&job, 1, s));
     int *st = mp->status.as<int>();
     CUMF_CUDA(launch_tc_gemm(mp->xb.p, mp->w1b.p, (int)rp, h, mp->dp, P + mp->off_b1, 1, mp->h1.p, 0, h,
                              mp->pre1.as<float>(), st, s));
@@ -282,40 +422,43 @@ int mlp_forward_ws(Mlp *mp, const float *X, int64_t rows, cudaStream_t s) {
     return CUMF_OK;
 }
 
-// Loss and gradients (into mp->grads) for rows [0, rows) with targets T (fp32 rows x d_out).
-int mlp_backward_ws(Mlp *mp, const float *T, int64_t rows, cudaStream_t s) {
+// Loss and gradients (into mp->grads) for rows [0, rows) with targets T (fp32 rows x d_out,
+// through perm as in mlp_forward_ws), after mlp_forward_ws on the same rows.
+int mlp_backward_ws(Mlp *mp, const float *T, int64_t rows, cudaStream_t s, const int32_t *perm = nullptr,
+                    const int *batch_idx = nullptr, int64_t batch = 0) {
     const int h = mp->h, dout = mp->d_out, dp = mp->dp;
     const int64_t rp = (rows + 127) / 128 * 128;
     float *G = mp->grads.as<float>();
+    float *part = mp->colws.as<float>();
     int *st = mp->status.as<int>();
     CUMF_CUDA(cudaMemsetAsync(mp->loss.p, 0, sizeof(double), s));
-    mse_grad_kernel<<<grid_of(rp * dout), kT, 0, s>>>(mp->y.as<float>(), T, rp, rows, dout, 1.f / (float)rows,
-                                                       mp->dy.as<__nv_bfloat16>(), mp->loss.as<double>());
+    // layer 3: dY (and dY^T, db3), dW3 = dY^T H2, dH2 = dY W3
+    mse_grad_t_kernel<<<tiles_of(rp, dout), kTileBlock, 0, s>>>(
+        mp->y.as<float>(), T, perm, batch_idx, batch, (int)rp, (int)rows, dout, 1.f / (float)rows,
+        mp->dy.as<__nv_bfloat16>(), mp->dyt.as<__nv_bfloat16>(), part, mp->loss.as<double>());
     CUMF_CUDA(cudaGetLastError());
-    // layer 3: dW3 = dY^T H2, db3 = colsum(dY), dH2 = dY W3
-    CUMF_CUDA(transpose(mp->dy.p, (int)rp, dout, mp->dyt.p, s));
+    CUMF_CUDA(colsum_finish(mp, rp, dout, G + mp->off_b3, s));
     CUMF_CUDA(transpose(mp->h2.p, (int)rp, h, mp->h2t.p, s));
     CUMF_CUDA(launch_tc_gemm(mp->dyt.p, mp->h2t.p, dout, h, (int)rp, nullptr, 0, G + mp->off_w3, 1, h, nullptr, st, s));
-    colsum_kernel<<<(dout + 127) / 128, 128, 0, s>>>(mp->dy.as<__nv_bfloat16>(), rp, dout, G + mp->off_b3);
     CUMF_CUDA(launch_tc_gemm(mp->dy.p, mp->w3t.p, (int)rp, h, dout, nullptr, 0, mp->dh2.p, 1, h, nullptr, st, s));
-    gelu_back_kernel<<<grid_of(rp * h), kT, 0, s>>>(mp->dh2.as<float>(), mp->pre2.as<float>(), rp, rows, h,
-                                                     mp->dp2.as<__nv_bfloat16>());
     // layer 2
-    CUMF_CUDA(transpose(mp->dp2.p, (int)rp, h, mp->dp2t.p, s));
+    gelu_back_t_kernel<<<tiles_of(rp, h), kTileBlock, 0, s>>>(mp->dh2.as<float>(), mp->pre2.as<float>(), (int)rp,
+                                                              (int)rows, h, mp->dp2.as<__nv_bfloat16>(),
+                                                              mp->dp2t.as<__nv_bfloat16>(), part);
+    CUMF_CUDA(cudaGetLastError());
+    CUMF_CUDA(colsum_finish(mp, rp, h, G + mp->off_b2, s));
     CUMF_CUDA(transpose(mp->h1.p, (int)rp, h, mp->h1t.p, s));
     CUMF_CUDA(launch_tc_gemm(mp->dp2t.p, mp->h1t.p, h, h, (int)rp, nullptr, 0, G + mp->off_w2, 1, h, nullptr, st, s));
-    colsum_kernel<<<(h + 127) / 128, 128, 0, s>>>(mp->dp2.as<__nv_bfloat16>(), rp, h, G + mp->off_b2);
     CUMF_CUDA(launch_tc_gemm(mp->dp2.p, mp->w2t.p, (int)rp, h, h, nullptr, 0, mp->dh1.p, 1, h, nullptr, st, s));
-    gelu_back_kernel<<<grid_of(rp * h), kT, 0, s>>>(mp->dh1.as<float>(), mp->pre1.as<float>(), rp, rows, h,
-                                                     mp->dp1.as<__nv_bfloat16>());
     // layer 1 (padded input columns give zero gradient columns, dropped on copy)
-    CUMF_CUDA(transpose(mp->dp1.p, (int)rp, h, mp->dp1t.p, s));
-    CUMF_CUDA(transpose(mp->xb.p, (int)rp, dp, mp->xbt.p, s));
+    gelu_back_t_kernel<<<tiles_of(rp, h), kTileBlock, 0, s>>>(mp->dh1.as<float>(), mp->pre1.as<float>(), (int)rp,
+                                                              (int)rows, h, mp->dp1.as<__nv_bfloat16>(),
+                                                              mp->dp1t.as<__nv_bfloat16>(), part);
+    CUMF_CUDA(cudaGetLastError());
+    CUMF_CUDA(colsum_finish(mp, rp, h, G + mp->off_b1, s));
     CUMF_CUDA(launch_tc_gemm(mp->dp1t.p, mp->xbt.p, h, dp, (int)rp, nullptr, 0, mp->gw1p.p, 1, dp, nullptr, st, s));
     CUMF_CUDA(cudaMemcpy2DAsync(G + mp->off_w1, mp->d_in * sizeof(float), mp->gw1p.p, dp * sizeof(float),
                                 mp->d_in * sizeof(float), h, cudaMemcpyDeviceToDevice, s));
-    colsum_kernel<<<(h + 127) / 128, 128, 0, s>>>(mp->dp1.as<__nv_bfloat16>(), rp, h, G + mp->off_b1);
-    CUMF_CUDA(cudaGetLastError());
     return CUMF_OK;
 }
 
@@ -438,48 +581,119 @@ int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, 
     Mlp *mp = static_cast<Mlp *>(mlp);
     if (!mp || !d_X || !d_T || rows <= 0 || epochs < 0 || batch <= 0)
         return fail(CUMF_ERR_ARG, "mlp_train: bad arguments");
-    cudaStream_t s = (cudaStream_t)stream;
-    DevBuf xs, ts, perm_d;
-    CUMF_CUDA(xs.alloc((size_t)batch * mp->d_in * 4));
-    CUMF_CUDA(ts.alloc((size_t)batch * mp->d_out * 4));
+    if (rows > 0x7fffffffll) return fail(CUMF_ERR_ARG, "mlp_train: more than 2^31 - 1 rows");
+    if (final_loss) *final_loss = 0;
+    if (epochs == 0) return CUMF_OK;
+    if (batch > rows) batch = (int)rows;
+    const int64_t full = rows / batch, tail = rows % batch;
+    if (int rc = mlp_ensure(mp, batch)) return rc;  // the workspace, before any capture
+
+    // Device state of the replayed step: Adam's step count and corrections, the batch index
+    // into the epoch's permutation, the epoch's loss.
+    struct State {
+        int64_t step;
+        int batch_idx;
+        int pad;
+        double loss_sum;
+    };
+    DevBuf perm_d, state;
     CUMF_CUDA(perm_d.alloc((size_t)rows * 4));
-    std::vector<int32_t> perm(rows);
-    GlibcRand rng((uint32_t)seed);
-    double last = 0;
-    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    for (int e = 0; e < epochs; ++e) {
-        for (int64_t i = 0; i < rows; ++i) perm[i] = (int32_t)i;
-        glibc_random_shuffle(perm.data(), rows, rng);
-        CUMF_CUDA(cudaMemcpyAsync(perm_d.p, perm.data(), rows * 4, cudaMemcpyHostToDevice, s));
-        double sum = 0;
-        int64_t seen = 0;
-        for (int64_t r0 = 0; r0 < rows; r0 += batch) {
-            const int64_t r = std::min<int64_t>(batch, rows - r0);
-            gather_rows_kernel<<<grid_of(r * mp->d_in), kT, 0, s>>>(d_X, mp->d_in, perm_d.as<int32_t>() + r0, r,
-                                                                     xs.as<float>());
-            gather_rows_kernel<<<grid_of(r * mp->d_out), kT, 0, s>>>(d_T, mp->d_out, perm_d.as<int32_t>() + r0, r,
-                                                                      ts.as<float>());
-            if (int rc = mlp_forward_ws(mp, xs.as<float>(), r, s)) return rc;
-            if (int rc = mlp_backward_ws(mp, ts.as<float>(), r, s)) return rc;
-            ++mp->step;
-            const float c1 = 1.f - powf(b1, (float)mp->step), c2 = 1.f - powf(b2, (float)mp->step);
-            adam_kernel<<<grid_of(mp->count), kT, 0, s>>>(mp->params.as<float>(), mp->grads.as<float>(),
-                                                          mp->m1.as<float>(), mp->m2.as<float>(), mp->count, lr, b1,
-                                                          b2, eps, c1, c2);
-            CUMF_CUDA(cudaGetLastError());
-            if (int rc = mlp_refresh(mp, s)) return rc;
-            if (e == epochs - 1) {
-                double l = 0;
-                CUMF_CUDA(cudaMemcpyAsync(&l, mp->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-                CUMF_CUDA(cudaStreamSynchronize(s));
-                sum += l;
-                seen += r;
-            }
+    CUMF_CUDA(state.alloc(sizeof(State)));
+    State *st = state.as<State>();
+    struct Host {
+        void *p[2] = {nullptr, nullptr};
+        ~Host() {
+            for (void *x : p)
+                if (x) cudaFreeHost(x);
         }
-        if (e == epochs - 1 && seen) last = sum / (double)seen;
+    } perm_h;
+    for (int k = 0; k < 2; ++k) CUMF_CUDA(cudaMallocHost(&perm_h.p[k], (size_t)rows * 4));
+    // A private stream (capture is not possible on the legacy default stream), ordered after
+    // the caller's stream and before its later work.
+    struct Res {
+        cudaStream_t ws = nullptr;
+        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+        cudaGraphExec_t exec[2] = {nullptr, nullptr};
+        ~Res() {
+            for (cudaGraphExec_t x : exec)
+                if (x) cudaGraphExecDestroy(x);
+            for (cudaEvent_t x : ev)
+                if (x) cudaEventDestroy(x);
+            if (ws) cudaStreamDestroy(ws);
+        }
+    } res;
+    CUMF_CUDA(cudaStreamCreateWithFlags(&res.ws, cudaStreamNonBlocking));
+    for (cudaEvent_t &x : res.ev) CUMF_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    cudaStream_t user = (cudaStream_t)stream, ws = res.ws;
+    CUMF_CUDA(cudaEventRecord(res.ev[0], user));
+    CUMF_CUDA(cudaStreamWaitEvent(ws, res.ev[0], 0));
+    const State init = {mp->step, 0, 0, 0.0};
+    CUMF_CUDA(cudaMemcpyAsync(st, &init, sizeof(State), cudaMemcpyHostToDevice, ws));
+    CUMF_CUDA(cudaStreamSynchronize(ws));  // `init` is a host local
+
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    // One training step of r rows at the batch the device index names.
+    auto enqueue_step = [&](int64_t r) -> int {
+        const int32_t *perm = perm_d.as<int32_t>();
+        if (int rc = mlp_forward_ws(mp, d_X, r, ws, perm, &st->batch_idx, batch)) return rc;
+        if (int rc = mlp_backward_ws(mp, d_T, r, ws, perm, &st->batch_idx, batch)) return rc;
+        adam_kernel<<<grid_of(mp->count), kT, 0, ws>>>(mp->params.as<float>(), mp->grads.as<float>(),
+                                                       mp->m1.as<float>(), mp->m2.as<float>(), mp->count, lr, b1, b2,
+                                                       eps, &st->step);
+        if (int rc = mlp_refresh(mp, ws)) return rc;
+        step_end_kernel<<<1, 1, 0, ws>>>(&st->step, &st->batch_idx, mp->loss.as<double>(), &st->loss_sum);
+        CUMF_CUDA(cudaGetLastError());
+        return CUMF_OK;
+    };
+    // Capture the full-batch step and the last, shorter one; replay them every epoch.
+    auto capture = [&](int64_t r, cudaGraphExec_t *exec) -> int {
+        CUMF_CUDA(cudaStreamBeginCapture(ws, cudaStreamCaptureModeRelaxed));
+        const int rc = enqueue_step(r);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ws, &g);
+        if (rc != CUMF_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc != CUMF_OK ? rc : cuda_fail(e, "mlp_train: capture");
+        }
+        const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+        cudaGraphDestroy(g);
+        CUMF_CUDA(ei);
+        return CUMF_OK;
+    };
+    if (full > 0)
+        if (int rc = capture(batch, &res.exec[0])) return rc;
+    if (tail > 0)
+        if (int rc = capture(tail, &res.exec[1])) return rc;
+
+    // Permutations from one glibc rand() stream, epoch by epoch; the next epoch's is drawn on
+    // the host while the device runs the current one (two pinned buffers).
+    GlibcRand rng((uint32_t)seed);
+    auto draw = [&](int32_t *perm) {
+        for (int64_t i = 0; i < rows; ++i) perm[i] = (int32_t)i;
+        glibc_random_shuffle(perm, rows, rng);
+    };
+    draw(static_cast<int32_t *>(perm_h.p[0]));
+    for (int e = 0; e < epochs; ++e) {
+        const int k = e & 1;
+        CUMF_CUDA(cudaMemsetAsync(&st->batch_idx, 0, sizeof(int), ws));
+        CUMF_CUDA(cudaMemsetAsync(&st->loss_sum, 0, sizeof(double), ws));
+        CUMF_CUDA(cudaMemcpyAsync(perm_d.p, perm_h.p[k], (size_t)rows * 4, cudaMemcpyHostToDevice, ws));
+        CUMF_CUDA(cudaEventRecord(res.ev[1 + k], ws));  // perm_h[k] may be redrawn after this
+        for (int64_t i = 0; i < full; ++i) CUMF_CUDA(cudaGraphLaunch(res.exec[0], ws));
+        if (tail > 0) CUMF_CUDA(cudaGraphLaunch(res.exec[1], ws));
+        if (e + 1 < epochs) {
+            CUMF_CUDA(cudaEventSynchronize(res.ev[1 + (k ^ 1)]));
+            draw(static_cast<int32_t *>(perm_h.p[k ^ 1]));
+        }
     }
-    if (int rc = mlp_check_status(mp, s)) return rc;
-    if (final_loss) *final_loss = last;
+    mp->step += (int64_t)epochs * (full + (tail > 0 ? 1 : 0));
+    double sum = 0;
+    CUMF_CUDA(cudaMemcpyAsync(&sum, &st->loss_sum, sizeof(double), cudaMemcpyDeviceToHost, ws));
+    if (int rc = mlp_check_status(mp, ws)) return rc;  // synchronizes ws
+    CUMF_CUDA(cudaEventRecord(res.ev[3], ws));
+    CUMF_CUDA(cudaStreamWaitEvent(user, res.ev[3], 0));
+    if (final_loss) *final_loss = sum / (double)rows;
     return CUMF_OK;
 }
 

@@ -71,3 +71,25 @@ def test_user_features_match_fp64(lib, cuda):
     ref = mlp_oracle.user_features(rec, Q, m, k)
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
     assert (got[-10:] == 0).all()
+
+
+def test_mlp_training_with_a_short_last_batch_continues_across_calls(lib, cuda):
+    """Rows not a multiple of the batch (the last, shorter step is a second captured graph),
+    and a second call continuing from the first (Adam's step count carries over)."""
+    import torch
+    rng = np.random.default_rng(4)
+    rows = 3000
+    X = rng.standard_normal((rows, D_IN)).astype(np.float32)
+    A = rng.standard_normal((D_IN, D_OUT)).astype(np.float32) / np.sqrt(D_IN)
+    T = np.tanh(X @ A).astype(np.float32)
+    mlp = cm.MLP(D_IN, H, D_OUT, seed=7)
+    dX, dT = torch.from_numpy(X).to(cuda), torch.from_numpy(T).to(cuda)
+    before = mlp.loss_grad(dX.data_ptr(), dT.data_ptr(), rows)
+    first = mlp.train(dX.data_ptr(), dT.data_ptr(), rows, epochs=15, batch=512, lr=1e-3, seed=3)
+    mid = mlp.loss_grad(dX.data_ptr(), dT.data_ptr(), rows)
+    second = mlp.train(dX.data_ptr(), dT.data_ptr(), rows, epochs=15, batch=512, lr=1e-3, seed=4)
+    after = mlp.loss_grad(dX.data_ptr(), dT.data_ptr(), rows)
+    assert np.isfinite([first, second]).all()
+    assert mid < 0.3 * before and after < mid, (before, mid, after)
+    assert second < first, (first, second)
+    assert mlp.train(dX.data_ptr(), dT.data_ptr(), rows, epochs=0, batch=512, lr=1e-3, seed=5) == 0.0
