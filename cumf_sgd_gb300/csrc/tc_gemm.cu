@@ -612,29 +612,41 @@ cudaError_t launch_tc_gemm(const void *A, const void *B, int M, int N, int K, co
                            void *out, int out_f32, int ldo, float *pre_out, int *status, cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0 || (K % 8) != 0) return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15)) return cudaErrorInvalidValue;
-    const bool wide = N > 128;
-    const int BN = wide ? 256 : 128;
-    CUtensorMap ma, mb;
-    if (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, BN)) return cudaErrorInvalidValue;
-    const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + BN - 1) / BN;
+    const int sms = sm_count_of_current_device();
+    const int nsm = sms > 0 ? sms : 152;
+    const int tiles_m = (M + kTcBM - 1) / kTcBM;
     const int kt = (K + kTcBK - 1) / kTcBK;
     // Short K (at most 16 stages of 64): a 2-stage ring, so two CTAs share an SM and
     // one CTA's epilogue overlaps another's loads.  Long K: a 4-stage ring, one CTA per SM.
     const bool short_k = kt <= 16;
     // Split K when the output has too few tiles to fill the GPU and K is long (weight
     // gradients): about one wave of CTAs, each with at least 8 stages.
-    int splits = 1;
     const bool plain = out_f32 && !bias && act == 0 && !pre_out;
-    if (plain && !short_k && tiles_m * tiles_n < 152) {
-        splits = std::max(1, std::min(kt / 8, 152 / (tiles_m * tiles_n)));
-        if (splits > 1) {
-            cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
-            if (e != cudaSuccess) return e;
-        }
+    auto splits_for = [&](long long tiles) -> int {
+        if (!plain || short_k || tiles >= nsm) return 1;
+        return (int)std::max(1ll, std::min<long long>(kt / 8, nsm / tiles));
+    };
+    // 128 x 256 tiles (one A tile feeds twice the columns) unless they leave most of a wave
+    // idle: 128 x 128 tiles when those give at least 1.5 times the CTAs and the wide ones do not
+    // fill the SMs (the MLP's 4096-row batches: 64 wide tiles, or weight gradients whose split
+    // is capped by K).
+    bool wide = N > 128;
+    if (wide) {
+        const long long tw = (long long)tiles_m * ((N + 255) / 256), tn = (long long)tiles_m * ((N + 127) / 128);
+        const long long cw = tw * splits_for(tw), cn = tn * splits_for(tn);
+        wide = cw >= nsm || 2 * cn < 3 * cw;
+    }
+    const int BN = wide ? 256 : 128;
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, A, M, K, kTcBM) || !make_map(&mb, B, N, K, BN)) return cudaErrorInvalidValue;
+    const int tiles_n = (N + BN - 1) / BN;
+    const int splits = splits_for((long long)tiles_m * tiles_n);
+    if (splits > 1) {
+        cudaError_t e = cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)N * 4, M, s);
+        if (e != cudaSuccess) return e;
     }
     // Enough output tiles for two per SM: the persistent kernel, whose epilogues overlap the
     // next tiles' loads and MMAs.
-    const int sms = sm_count_of_current_device();
     if (splits == 1 && sms > 0 && (long long)tiles_m * tiles_n >= 2ll * sms) {
         const int g = std::min(tiles_m * tiles_n, sms);
         return wide ? launch_persistent<256, 4>(g, ma, mb, M, N, K, bias, act, out, out_f32, ldo, pre_out, status, s)
