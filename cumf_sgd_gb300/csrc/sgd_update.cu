@@ -63,6 +63,45 @@ __device__ __forceinline__ uint4 opaque(uint4 w) {
     return w;
 }
 
+// The new rows of one record: p + lr*(e*q - lp*p) and q + lr*(e*p_old - lq*q)
+// (warp32.h:89-99), in fp32, stored rounded to the storage type (stochastically when SR; the
+// random bits of element pair h of word i of this lane are lowbias32(key + 2*pair) for p and
+// lowbias32(key + 2*pair + 1) for q).  kUpdateQ = false (item rows frozen): wq is fq and none
+// of q's arithmetic or random bits is computed.
+template <class C, int NV, bool SR, bool kUpdateQ>
+__device__ __forceinline__ void update_rows(const uint4 (&fp)[NV], const uint4 (&fq)[NV], uint4 (&wp)[NV],
+                                            uint4 (&wq)[NV], float lr, float err, float lp, float lq, uint32_t key,
+                                            int lane) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const uint4 fpi = opaque(fp[i]), fqi = opaque(fq[i]);
+#pragma unroll
+        for (int h = 0; h < C::kPairs; ++h) {
+            const float2 pp = C::get(fpi, h), qq = C::get(fqi, h);
+            const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
+            const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
+            if (kUpdateQ) {
+                const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
+                const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
+                if (SR) {
+                    const uint32_t pair = (uint32_t)(((lane * NV + i) * C::kPairs + h) * 2);
+                    C::put_sr(wp[i], h, px, py, lowbias32(key + pair));
+                    C::put_sr(wq[i], h, qx, qy, lowbias32(key + pair + 1u));
+                } else {
+                    C::put(wp[i], h, px, py);
+                    C::put(wq[i], h, qx, qy);
+                }
+            } else if (SR) {
+                const uint32_t pair = (uint32_t)(((lane * NV + i) * C::kPairs + h) * 2);
+                C::put_sr(wp[i], h, px, py, lowbias32(key + pair));
+            } else {
+                C::put(wp[i], h, px, py);
+            }
+        }
+        if (!kUpdateQ) wq[i] = fq[i];
+    }
+}
+
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem, uint64_t pol) {
     const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "l"(pol)
@@ -210,30 +249,16 @@ sgd_hogwild_kernel(const UpdateArgs a) {
                         key = round_key ^ lowbias32(sample);
                     }
                     uint4 wp[NV], wq[NV];
+                    // Frozen item rows: the stochastic-rounding kernels skip q's arithmetic and
+                    // random bits; the others compute q and keep the old row (fewer registers).
+                    if (SR && a.freeze_q) {
+                        update_rows<C, NV, SR, false>(fp, fq, wp, wq, lr, err, lp, lq, key, lane);
+                    } else {
+                        update_rows<C, NV, SR, true>(fp, fq, wp, wq, lr, err, lp, lq, key, lane);
+                        if (a.freeze_q) {
 #pragma unroll
-                    for (int i = 0; i < NV; ++i) {
-                        const uint4 fpi = opaque(fp[i]), fqi = opaque(fq[i]);
-#pragma unroll
-                        for (int h = 0; h < C::kPairs; ++h) {
-                            const float2 pp = C::get(fpi, h), qq = C::get(fqi, h);
-                            // p + lr*(e*q - lp*p), q + lr*(e*p_old - lq*q)  (warp32.h:89-99)
-                            const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
-                            const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
-                            const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
-                            const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
-                            if (SR) {
-                                const uint32_t pair = (uint32_t)(((lane * NV + i) * C::kPairs + h) * 2);
-                                C::put_sr(wp[i], h, px, py, lowbias32(key + pair));
-                                C::put_sr(wq[i], h, qx, qy, lowbias32(key + pair + 1u));
-                            } else {
-                                C::put(wp[i], h, px, py);
-                                C::put(wq[i], h, qx, qy);
-                            }
+                            for (int i = 0; i < NV; ++i) wq[i] = fq[i];
                         }
-                    }
-                    if (a.freeze_q) {
-#pragma unroll
-                        for (int i = 0; i < NV; ++i) wq[i] = fq[i];
                     }
 #pragma unroll
                     for (int i = 0; i < NV; ++i) {
@@ -431,29 +456,14 @@ sgd_ring_kernel(const UpdateArgs a) {
                 const float err = r - s;
                 uint32_t key = 0;
                 if (SR) key = round_key ^ lowbias32((uint32_t)worker * (uint32_t)total + (uint32_t)x);
+                if (SR && a.freeze_q) {
+                    update_rows<C, NV, SR, false>(fp, fq, wp, wq, lr, err, lp, lq, key, lane);
+                } else {
+                    update_rows<C, NV, SR, true>(fp, fq, wp, wq, lr, err, lp, lq, key, lane);
+                    if (a.freeze_q) {
 #pragma unroll
-                for (int i = 0; i < NV; ++i) {
-                    const uint4 fpi = opaque(fp[i]), fqi = opaque(fq[i]);
-#pragma unroll
-                    for (int h = 0; h < C::kPairs; ++h) {
-                        const float2 pp = C::get(fpi, h), qq = C::get(fqi, h);
-                        const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(lp, pp.x)), pp.x);
-                        const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(lp, pp.y)), pp.y);
-                        const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(lq, qq.x)), qq.x);
-                        const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(lq, qq.y)), qq.y);
-                        if (SR) {
-                            const uint32_t pair = (uint32_t)(((lane * NV + i) * C::kPairs + h) * 2);
-                            C::put_sr(wp[i], h, px, py, lowbias32(key + pair));
-                            C::put_sr(wq[i], h, qx, qy, lowbias32(key + pair + 1u));
-                        } else {
-                            C::put(wp[i], h, px, py);
-                            C::put(wq[i], h, qx, qy);
-                        }
+                        for (int i = 0; i < NV; ++i) wq[i] = fq[i];
                     }
-                }
-                if (a.freeze_q) {
-#pragma unroll
-                    for (int i = 0; i < NV; ++i) wq[i] = fq[i];
                 }
 #pragma unroll
                 for (int i = 0; i < NV; ++i) {

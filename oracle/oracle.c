@@ -302,7 +302,7 @@ static float dot_ref(const float *p, const float *q) {
 
 /* One SGD update of rows p, q with rating r (warp32.h:85-99), in the kernel's fma order. */
 static void update_rows(float *p, float *q, int k, float r, float lr, float lp, float lq, int kind,
-                        int sr, uint32_t key, int G, int dot_order) {
+                        int sr, uint32_t key, int G, int dot_order, int freeze_q) {
     const float s = dot_order == OR_DOT_REF ? dot_ref(p, q) : dot_lanes(p, q, k, G);
     const float err = r - s;
     for (int d = 0; d < k; d++) {
@@ -315,10 +315,10 @@ static void update_rows(float *p, float *q, int k, float r, float lr, float lp, 
             const uint32_t rp = (d & 1) ? (bp >> 16) : (bp & 0xffffu);
             const uint32_t rq = (d & 1) ? (bq >> 16) : (bq & 0xffffu);
             p[d] = kind == OR_HALF ? half_sr(pn, rp) : bf16_sr(pn, rp);
-            q[d] = kind == OR_HALF ? half_sr(qn, rq) : bf16_sr(qn, rq);
+            if (!freeze_q) q[d] = kind == OR_HALF ? half_sr(qn, rq) : bf16_sr(qn, rq);
         } else {
             p[d] = or_round_store(pn, kind);
-            q[d] = or_round_store(qn, kind);
+            if (!freeze_q) q[d] = or_round_store(qn, kind);
         }
     }
 }
@@ -338,7 +338,7 @@ static void run_batch(or_sgd_args *a, int ep, int w, int64_t b, int64_t batches,
             key = round_key ^ or_lowbias32(sample);
         }
         update_rows(a->P + (int64_t)x.u * a->k, a->Q + (int64_t)x.v * a->k, a->k, x.r, lr, a->lambda_p,
-                    a->lambda_q, a->kind, a->sr, key, a->lanes, a->dot_order);
+                    a->lambda_q, a->kind, a->sr, key, a->lanes, a->dot_order, a->freeze_q);
     }
 }
 
@@ -837,7 +837,7 @@ int64_t or_strata_epochs(const or_node *R, int64_t nnz, float *P, int32_t m, flo
                     }
                     const uint32_t key = sr ? (round_key ^ or_lowbias32((uint32_t)i)) : 0u;
                     update_rows(P + (int64_t)x.u * k, Q + (int64_t)x.v * k, k, x.r, lr[ep], lambda_p, lambda_q, kind,
-                                sr, key, lanes, OR_DOT_LANES);
+                                sr, key, lanes, OR_DOT_LANES, 0);
                 }
             }
         }

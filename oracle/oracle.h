@@ -93,6 +93,7 @@ typedef struct or_sgd_args {
     float lambda_p, lambda_q;
     uint64_t seed;
     int64_t skipped;     /* out: records with an id out of range */
+    int freeze_q;        /* 1: item rows are read but never written (user fold-in) */
 } or_sgd_args;
 void or_sgd_epochs(or_sgd_args *a);
 

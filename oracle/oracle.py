@@ -60,7 +60,8 @@ class _SgdArgs(C.Structure):
                 ("sr", C.c_int), ("num_workers", C.c_int), ("lanes", C.c_int),
                 ("dot_order", C.c_int), ("order", C.c_int), ("lr", C.c_void_p),
                 ("first_epoch", C.c_int), ("n_epochs", C.c_int), ("lambda_p", C.c_float),
-                ("lambda_q", C.c_float), ("seed", C.c_uint64), ("skipped", C.c_int64)]
+                ("lambda_q", C.c_float), ("seed", C.c_uint64), ("skipped", C.c_int64),
+                ("freeze_q", C.c_int)]
 
 
 class _TrainArgs(C.Structure):
@@ -182,15 +183,16 @@ def init_factors(rows: int, k: int, precision: str, seed: int, tag: int) -> np.n
 def sgd_epochs(records: np.ndarray, P: np.ndarray, Q: np.ndarray, precision: str, num_workers: int,
                lr: np.ndarray, first_epoch: int, n_epochs: int, lambda_p: float, lambda_q: float,
                seed: int, lanes: int = 16, dot_order: int = OR_DOT_LANES,
-               order: int = OR_ORDER_ROUND_ROBIN) -> int:
-    """Serial batch-Hogwild epochs in place on fp32 arrays P, Q; returns skipped records."""
+               order: int = OR_ORDER_ROUND_ROBIN, freeze_q: int = 0) -> int:
+    """Serial batch-Hogwild epochs in place on fp32 arrays P, Q (freeze_q: Q is read, never
+    written); returns skipped records."""
     rec = np.ascontiguousarray(records)
     lr = np.ascontiguousarray(lr, dtype=np.float32)
     kind, sr = KIND[precision]
     a = _SgdArgs(R=_ptr(rec), nnz=len(rec), P=_ptr(P), m=P.shape[0], Q=_ptr(Q), n=Q.shape[0],
                  k=P.shape[1], kind=kind, sr=sr, num_workers=num_workers, lanes=lanes,
                  dot_order=dot_order, order=order, lr=_ptr(lr), first_epoch=first_epoch,
-                 n_epochs=n_epochs, lambda_p=lambda_p, lambda_q=lambda_q, seed=seed)
+                 n_epochs=n_epochs, lambda_p=lambda_p, lambda_q=lambda_q, seed=seed, freeze_q=freeze_q)
     lib().or_sgd_epochs(C.byref(a))
     return a.skipped
 

@@ -63,7 +63,7 @@ def test_init_factors_bit_exact(lib, orc, cuda, precision, k):
     assert got.min() > 0 and got.max() <= np.float32(1 / np.sqrt(k)) * 1.001
 
 
-def run_gpu_epochs(cuda, rec, m, n, k, precision, workers, lanes, lr, epochs, lp, lq, seed, ring=-1):
+def run_gpu_epochs(cuda, rec, m, n, k, precision, workers, lanes, lr, epochs, lp, lq, seed, ring=-1, freeze_q=0):
     torch = tt()
     d_R = dev(rec, cuda)
     P = torch.empty(m * k * elem(precision), dtype=torch.uint8, device=cuda)
@@ -73,7 +73,7 @@ def run_gpu_epochs(cuda, rec, m, n, k, precision, workers, lanes, lr, epochs, lp
     d_lr = torch.from_numpy(lr).to(cuda)
     status = torch.zeros(1, dtype=torch.int32, device=cuda)
     cm.sgd_update(d_R.data_ptr(), len(rec), P.data_ptr(), m, Q.data_ptr(), n, k, precision, workers, lanes,
-                  d_lr.data_ptr(), 0, epochs, lp, lq, seed, status.data_ptr(), ring=ring)
+                  d_lr.data_ptr(), 0, epochs, lp, lq, seed, status.data_ptr(), ring=ring, freeze_q=freeze_q)
     torch.cuda.synchronize()
     return storage_to_float(P, precision, m, k), storage_to_float(Q, precision, n, k), int(status.item())
 
@@ -97,6 +97,27 @@ def test_single_worker_sgd_bit_exact(lib, orc, cuda, precision, k, lanes, ring):
     assert skipped == 0
     np.testing.assert_array_equal(Pg, P)
     np.testing.assert_array_equal(Qg, Q)
+
+
+@pytest.mark.parametrize("ring", [0, 1], ids=["regs", "ring"])
+@pytest.mark.parametrize("precision", PRECS)
+@pytest.mark.parametrize("k", [128, 64, 256])
+def test_single_worker_fold_in_bit_exact(lib, orc, cuda, precision, k, ring):
+    """Fold-in epochs (item rows frozen): the stochastic-rounding kernels skip the item rows'
+    arithmetic and random bits; user rows must still match the oracle bit for bit and the item
+    rows stay as initialised."""
+    m, n, nnz = 60, 40, 2500
+    rec = small_problem(m, n, nnz, 19)
+    lr = orc.lr_table(0.08, 0.3, 0.0, 8)
+    Pg, Qg, st = run_gpu_epochs(cuda, rec, m, n, k, precision, 1, 0, lr, 3, 0.05, 0.04, 6, ring, freeze_q=1)
+    assert st == 0
+    P = orc.init_factors(m, k, precision, 6, 1)
+    Q = orc.init_factors(n, k, precision, 6, 2)
+    Q0 = Q.copy()
+    orc.sgd_epochs(rec, P, Q, precision, 1, lr, 0, 3, 0.05, 0.04, 6, lanes=default_lanes(k, precision), freeze_q=1)
+    np.testing.assert_array_equal(Q, Q0)
+    np.testing.assert_array_equal(Qg, Q0)
+    np.testing.assert_array_equal(Pg, P)
 
 
 def default_lanes(k, precision):
