@@ -79,16 +79,25 @@ __global__ void user_qsum_kernel(const cumf_node *R, int64_t nnz, int32_t m, int
     }
 }
 
-__global__ void user_scalar_kernel(int32_t m, int k, const float *deg, const float *sum, const float *sum2, float *X,
-                                   int ldx) {
-    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < m; u += (int64_t)gridDim.x * blockDim.x) {
+// x[u] = (acc[u][0:k], log(1 + deg)/4, (mean - 3)/2, var/2) for the m users (ldx = k + 3).
+__global__ void user_finish_kernel(int32_t m, int k, const float *acc, const float *deg, const float *sum,
+                                   const float *sum2, float *X, int ldx) {
+    const int64_t total = (int64_t)m * ldx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / ldx;
+        const int c = (int)(i - u * ldx);
+        if (c < k) {
+            X[i] = acc[u * k + c];
+            continue;
+        }
         const float d = deg[u];
         const float mean = d > 0 ? sum[u] / d : 0.f;
-        const float var = d > 0 ? fmaxf(sum2[u] / d - mean * mean, 0.f) : 0.f;
-        float *x = X + u * ldx;
-        x[k] = logf(1.f + d) * 0.25f;
-        x[k + 1] = d > 0 ? (mean - 3.f) * 0.5f : 0.f;
-        x[k + 2] = var * 0.5f;
+        if (c == k)
+            X[i] = logf(1.f + d) * 0.25f;
+        else if (c == k + 1)
+            X[i] = d > 0 ? (mean - 3.f) * 0.5f : 0.f;
+        else
+            X[i] = (d > 0 ? fmaxf(sum2[u] / d - mean * mean, 0.f) : 0.f) * 0.5f;
     }
 }
 
@@ -318,7 +327,8 @@ struct Mlp {
     DevBuf status;
     int64_t step = 0;
     // workspace for one batch of up to cap rows
-    int64_t cap = 0;
+    int64_t cap = 0;      // rows of the backward buffers
+    int64_t cap_fwd = 0;  // rows of the forward buffers
     DevBuf xb, h1, h2, pre1, pre2, y, dy, dyt, h2t, h1t, xbt, dh2, dp2, dp2t, dh1, dp1, dp1t, loss;
     DevBuf gw1p;  // gradient of W1 in padded layout [h][dp]
     DevBuf colws; // (cap / 32) x max(h, d_out) tile column sums
@@ -326,17 +336,22 @@ struct Mlp {
 
 namespace {
 
-int mlp_ensure(Mlp *mp, int64_t rows) {
-    if (rows <= mp->cap) return CUMF_OK;
+// Workspace for batches of up to `rows` rows: the forward buffers, and with `train` also
+// those of the backward pass (the activations' transposes, pre-activations, gradients).
+int mlp_ensure(Mlp *mp, int64_t rows, bool train) {
     const int64_t r = (rows + 127) / 128 * 128;
     const size_t b2 = 2;
     const int h = mp->h, dp = mp->dp, dout = mp->d_out;
-    CUMF_CUDA(mp->xb.alloc(r * dp * b2));
-    CUMF_CUDA(mp->h1.alloc(r * h * b2));
-    CUMF_CUDA(mp->h2.alloc(r * h * b2));
+    if (rows > mp->cap_fwd) {
+        CUMF_CUDA(mp->xb.alloc(r * dp * b2));
+        CUMF_CUDA(mp->h1.alloc(r * h * b2));
+        CUMF_CUDA(mp->h2.alloc(r * h * b2));
+        CUMF_CUDA(mp->y.alloc(r * dout * 4));
+        mp->cap_fwd = r;
+    }
+    if (!train || rows <= mp->cap) return CUMF_OK;
     CUMF_CUDA(mp->pre1.alloc(r * h * 4));
     CUMF_CUDA(mp->pre2.alloc(r * h * 4));
-    CUMF_CUDA(mp->y.alloc(r * dout * 4));
     CUMF_CUDA(mp->dy.alloc(r * dout * b2));
     CUMF_CUDA(mp->dyt.alloc(r * dout * b2));
     CUMF_CUDA(mp->h2t.alloc(r * h * b2));
@@ -402,21 +417,22 @@ int mlp_refresh(Mlp *mp, cudaStream_t s) {
 }
 
 // Forward over rows [0, rows) of X (fp32, rows x d_in; with perm, row r is X[perm[*batch_idx *
-// batch + r]]); Y (fp32 rows x d_out) in mp->y.  Also leaves X's bf16 transpose for backward.
-int mlp_forward_ws(Mlp *mp, const float *X, int64_t rows, cudaStream_t s, const int32_t *perm = nullptr,
+// batch + r]]); Y (fp32 rows x d_out) in mp->y.  train: also X's bf16 transpose and the
+// pre-activations, which the backward pass uses.
+int mlp_forward_ws(Mlp *mp, const float *X, int64_t rows, cudaStream_t s, bool train, const int32_t *perm = nullptr,
                    const int *batch_idx = nullptr, int64_t batch = 0) {
-    if (int rc = mlp_ensure(mp, rows)) return rc;
+    if (int rc = mlp_ensure(mp, rows, train)) return rc;
     const float *P = mp->params.as<float>();
     const int h = mp->h;
     const int64_t rp = (rows + 127) / 128 * 128;  // padding rows are zero
     const ConvertJob job = convert_job(X, mp->d_in, perm, batch_idx, batch, (int)rows, (int)rp, mp->dp, mp->xb.p,
-                                       mp->xbt.p);
+                                       train ? mp->xbt.p : nullptr);
     CUMF_CUDA(convert(&job, 1, s));
     int *st = mp->status.as<int>();
     CUMF_CUDA(launch_tc_gemm(mp->xb.p, mp->w1b.p, (int)rp, h, mp->dp, P + mp->off_b1, 1, mp->h1.p, 0, h,
-                             mp->pre1.as<float>(), st, s));
+                             train ? mp->pre1.as<float>() : nullptr, st, s));
     CUMF_CUDA(launch_tc_gemm(mp->h1.p, mp->w2b.p, (int)rp, h, h, P + mp->off_b2, 1, mp->h2.p, 0, h,
-                             mp->pre2.as<float>(), st, s));
+                             train ? mp->pre2.as<float>() : nullptr, st, s));
     CUMF_CUDA(launch_tc_gemm(mp->h2.p, mp->w3b.p, (int)rp, mp->d_out, h, P + mp->off_b3, 0, mp->y.p, 1, mp->d_out,
                              nullptr, st, s));
     return CUMF_OK;
@@ -557,7 +573,7 @@ int cumf_mlp_forward(void *mlp, const float *d_X, int64_t rows, float *d_Y, void
     const int64_t chunk = 1 << 16;
     for (int64_t r0 = 0; r0 < rows; r0 += chunk) {
         const int64_t r = std::min(chunk, rows - r0);
-        if (int rc = mlp_forward_ws(mp, d_X + r0 * mp->d_in, r, s)) return rc;
+        if (int rc = mlp_forward_ws(mp, d_X + r0 * mp->d_in, r, s, false)) return rc;
         CUMF_CUDA(cudaMemcpyAsync(d_Y + r0 * mp->d_out, mp->y.p, r * mp->d_out * 4, cudaMemcpyDeviceToDevice, s));
     }
     return mlp_check_status(mp, s);
@@ -567,7 +583,7 @@ int cumf_mlp_loss_grad(void *mlp, const float *d_X, const float *d_T, int64_t ro
     Mlp *mp = static_cast<Mlp *>(mlp);
     if (!mp || !d_X || !d_T || rows <= 0) return fail(CUMF_ERR_ARG, "mlp_loss_grad: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    if (int rc = mlp_forward_ws(mp, d_X, rows, s)) return rc;
+    if (int rc = mlp_forward_ws(mp, d_X, rows, s, true)) return rc;
     if (int rc = mlp_backward_ws(mp, d_T, rows, s)) return rc;
     double l = 0;
     CUMF_CUDA(cudaMemcpyAsync(&l, mp->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -586,7 +602,7 @@ int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, 
     if (epochs == 0) return CUMF_OK;
     if (batch > rows) batch = (int)rows;
     const int64_t full = rows / batch, tail = rows % batch;
-    if (int rc = mlp_ensure(mp, batch)) return rc;  // the workspace, before any capture
+    if (int rc = mlp_ensure(mp, batch, true)) return rc;  // the workspace, before any capture
 
     // Device state of the replayed step: Adam's step count and corrections, the batch index
     // into the epoch's permutation, the epoch's loss.
@@ -635,7 +651,7 @@ int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, 
     // One training step of r rows at the batch the device index names.
     auto enqueue_step = [&](int64_t r) -> int {
         const int32_t *perm = perm_d.as<int32_t>();
-        if (int rc = mlp_forward_ws(mp, d_X, r, ws, perm, &st->batch_idx, batch)) return rc;
+        if (int rc = mlp_forward_ws(mp, d_X, r, ws, true, perm, &st->batch_idx, batch)) return rc;
         if (int rc = mlp_backward_ws(mp, d_T, r, ws, perm, &st->batch_idx, batch)) return rc;
         adam_kernel<<<grid_of(mp->count), kT, 0, ws>>>(mp->params.as<float>(), mp->grads.as<float>(),
                                                        mp->m1.as<float>(), mp->m2.as<float>(), mp->count, lr, b1, b2,
@@ -702,29 +718,26 @@ int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int3
     if (!d_Q || !d_X || m <= 0 || n <= 0 || k <= 0 || nnz < 0 || (nnz > 0 && !d_R))
         return fail(CUMF_ERR_ARG, "user_features: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    DevBuf deg, sum, sum2;
-    CUMF_CUDA(deg.alloc((size_t)m * 4));
-    CUMF_CUDA(sum.alloc((size_t)m * 4));
-    CUMF_CUDA(sum2.alloc((size_t)m * 4));
-    CUMF_CUDA(cudaMemsetAsync(deg.p, 0, (size_t)m * 4, s));
-    CUMF_CUDA(cudaMemsetAsync(sum.p, 0, (size_t)m * 4, s));
-    CUMF_CUDA(cudaMemsetAsync(sum2.p, 0, (size_t)m * 4, s));
-    // The centred mean accumulates in a k-wide buffer (16-byte aligned rows for the vector
-    // atomics), then lands in the (k+3)-wide feature rows beside the scalar features.
-    const int ldx = k + 3;
-    DevBuf acc;
-    CUMF_CUDA(acc.alloc((size_t)m * k * 4));
-    CUMF_CUDA(cudaMemsetAsync(acc.p, 0, (size_t)m * k * 4, s));
-    if (nnz > 0) {
-        user_stats_kernel<<<grid_of(nnz), kT, 0, s>>>(d_R, nnz, m, n, deg.as<float>(), sum.as<float>(),
-                                                       sum2.as<float>());
-        user_qsum_kernel<<<grid_of(nnz * 32), kT, 0, s>>>(d_R, nnz, m, n, d_Q, k, deg.as<float>(), sum.as<float>(),
-                                                           acc.as<float>(), k);
+    // One stream-ordered scratch: the centred mean accumulates in k-wide rows (16-byte aligned
+    // for the vector atomics), then degree, rating sum and sum of squares per user.
+    const size_t acc_bytes = (size_t)m * k * 4, scratch = acc_bytes + 3 * (size_t)m * 4;
+    void *buf = nullptr;
+    CUMF_CUDA(cudaMallocAsync(&buf, scratch, s));
+    float *acc = static_cast<float *>(buf);
+    float *deg = acc + (size_t)m * k, *sum = deg + m, *sum2 = sum + m;
+    cudaError_t e = cudaMemsetAsync(buf, 0, scratch, s);
+    if (e == cudaSuccess && nnz > 0) {
+        user_stats_kernel<<<grid_of(nnz), kT, 0, s>>>(d_R, nnz, m, n, deg, sum, sum2);
+        user_qsum_kernel<<<grid_of(nnz * 32), kT, 0, s>>>(d_R, nnz, m, n, d_Q, k, deg, sum, acc, k);
+        e = cudaGetLastError();
     }
-    CUMF_CUDA(cudaMemcpy2DAsync(d_X, (size_t)ldx * 4, acc.p, (size_t)k * 4, (size_t)k * 4, m,
-                                cudaMemcpyDeviceToDevice, s));
-    user_scalar_kernel<<<grid_of(m), kT, 0, s>>>(m, k, deg.as<float>(), sum.as<float>(), sum2.as<float>(), d_X, ldx);
-    CUMF_CUDA(cudaGetLastError());
+    if (e == cudaSuccess) {
+        user_finish_kernel<<<grid_of((int64_t)m * (k + 3)), kT, 0, s>>>(m, k, acc, deg, sum, sum2, d_X, k + 3);
+        e = cudaGetLastError();
+    }
+    const cudaError_t ef = cudaFreeAsync(buf, s);
+    CUMF_CUDA(e);
+    CUMF_CUDA(ef);
     CUMF_CUDA(cudaStreamSynchronize(s));
     return CUMF_OK;
 }
