@@ -326,7 +326,7 @@ struct Mlp {
     DevBuf w1b, w2b, w3b, w2t, w3t;
     DevBuf status;
     int64_t step = 0;
-    // workspace for one batch of up to cap rows
+    // workspace for batches of up to cap_fwd rows (forward) / cap rows (backward)
     int64_t cap = 0;      // rows of the backward buffers
     int64_t cap_fwd = 0;  // rows of the forward buffers
     DevBuf xb, h1, h2, pre1, pre2, y, dy, dyt, h2t, h1t, xbt, dh2, dp2, dp2t, dh1, dp1, dp1t, loss;
