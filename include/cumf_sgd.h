@@ -370,7 +370,10 @@ int cumf_mlp_forward(void *mlp, const float *d_X, int64_t rows, float *d_Y, void
 /* Mean-over-rows squared error against d_T and its gradients (kept in the handle). */
 int cumf_mlp_loss_grad(void *mlp, const float *d_X, const float *d_T, int64_t rows, double *loss, void *stream);
 /* Adam (0.9, 0.999) over shuffled mini-batches for `epochs` passes; *final_loss is the mean
- * loss of the last pass. */
+ * loss of the last pass (0 for epochs == 0).  One training step is captured as a CUDA graph
+ * and replayed per batch on a private stream ordered after `stream`; the next pass's
+ * permutation is drawn on the host while the device runs the current one.  rows < 2^31;
+ * batch > rows trains on whole passes.  Adam's step count carries over between calls. */
 int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, int epochs, int batch, float lr,
                    uint64_t seed, double *final_loss, void *stream);
 

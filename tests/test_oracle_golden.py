@@ -142,3 +142,24 @@ def test_criteria_oracle_matches_reference(orc):
                 assert np.isnan(got), (i, c)
             else:
                 assert abs(got - ref) <= 1e-6 * max(1.0, abs(ref)), (i, c, got, ref)
+
+
+def test_oracle_fold_in_freezes_items(orc):
+    """freeze_q: item rows are read, never written, and user rows still move (the GPU kernels
+    are compared with this bit for bit in test_single_worker_fold_in_bit_exact)."""
+    import cumf_sgd_gb300 as cm
+    rng = np.random.default_rng(3)
+    m, n, k = 30, 12, 64
+    rec = np.empty(600, dtype=cm.NODE_DTYPE)
+    rec["u"], rec["v"] = rng.integers(0, m, 600), rng.integers(0, n, 600)
+    rec["r"] = rng.integers(1, 6, 600).astype(np.float32)
+    lr = orc.lr_table(0.08, 0.3, 0.0, 4)
+    for precision in ("fp32", "fp16", "bf16", "bf16sr", "fp16sr"):
+        P0, Q0 = orc.init_factors(m, k, precision, 2, 1), orc.init_factors(n, k, precision, 2, 2)
+        P, Q = P0.copy(), Q0.copy()
+        orc.sgd_epochs(rec, P, Q, precision, 1, lr, 0, 2, 0.05, 0.05, 2, freeze_q=1)
+        assert np.array_equal(Q, Q0), precision
+        assert not np.array_equal(P, P0), precision
+        Pu, Qu = P0.copy(), Q0.copy()
+        orc.sgd_epochs(rec, Pu, Qu, precision, 1, lr, 0, 2, 0.05, 0.05, 2, freeze_q=0)
+        assert not np.array_equal(Qu, Q0) and not np.array_equal(Pu, P), precision
