@@ -92,18 +92,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """dram read+write bytes per launch of the update kernel, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "sgd_hogwild_c2.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the update kernel
+# at the c2 shape (one fp16 epoch, 100.86M samples, 29,184 workers), from one ncu capture of
+# this kernel (summary: profiles/sgd_hogwild_c2.md).  A constant: ncu cannot run inside the
+# timed bench, and the capture is redone whenever the kernel changes.
+UPDATE_KERNEL_DRAM_BYTES_C2 = 18.146e9
+UPDATE_KERNEL_DRAM_BYTES_SOURCE = "ncu capture of one c2 fp16 launch of sgd_hogwild_kernel<128,fp16,16>"
 
 
 class ClockSampler:
@@ -186,28 +180,98 @@ def cpu_port_baseline(train: np.ndarray, m: int, n: int, seconds_budget: float =
                       f"windows of the c2 train set, fp32 factors 480189x128 / 17770x128, {el:.1f} s"}
 
 
+def _reference_tools():
+    """oracle/ref_tools with the reference trainers built (on the GPU host from the sources
+    that oracle/ref_build.sh staged), or None."""
+    from oracle import oracle, ref_tools
+    try:
+        oracle.build_reference()
+    except Exception as e:  # reported by the caller as "not available"
+        print(json.dumps({"note": "reference tools not built", "why": repr(e)[:300]}), file=sys.stderr)
+    return ref_tools if ref_tools.available("mf-train", "mf-predict") else None
+
+
+def libmf_baseline(ref_tools, train, iters: int, threads: int, tmpdir: str, warm_iters: int = 0,
+                   test=None) -> dict:
+    """LIBMF mf-train (test/mf-train.cpp; the reference's CPU trainer) on the host cores:
+    `threads` threads, 2*threads+1 blocks, k=128, l2 0.05, `iters` iterations over `train`.
+    With warm_iters > 0 a first run of warm_iters iterations is subtracted, so the rate is
+    that of iterations warm_iters+1 .. iters (its "computation time" excludes file reading).
+    Returns updates/s and, with `test`, the RMSE printed by mf-predict -e 0."""
+    tr_path = os.path.join(tmpdir, "libmf_train.bin")
+    mp = os.path.join(tmpdir, "libmf.model")
+    ref_tools.write_records(train, tr_path)
+    t_warm = 0.0
+    if warm_iters > 0:
+        w = ref_tools.run_libmf(tr_path, mp, warm_iters, threads)
+        if w["rc"] != 0 or w["computation_s"] is None:
+            raise RuntimeError("mf-train failed: " + w["tail"])
+        t_warm = w["computation_s"]
+    r = ref_tools.run_libmf(tr_path, mp, iters, threads)
+    if r["rc"] != 0 or r["computation_s"] is None:
+        raise RuntimeError("mf-train failed: " + r["tail"])
+    timed = iters - warm_iters
+    secs = r["computation_s"] - t_warm
+    out = {"value": len(train) * timed / secs, "unit": "updates/s", "cores": threads, "kind": "reference",
+           "perf_line": r["perf"], "computation_s": r["computation_s"], "timed_iterations": timed,
+           "timed_s": secs, "build": ref_tools.build_info()}
+    if test is not None:
+        te_path = os.path.join(tmpdir, "libmf_test.bin")
+        ref_tools.write_records(test, te_path)
+        out["test_rmse_mf_predict"] = ref_tools.libmf_rmse(te_path, mp)
+        out["model_path"] = mp
+    return out
+
+
 def run_reference_arm(args):
+    """The reference's own CPU trainer, LIBMF mf-train, on the host cores (rank 0 only):
+    W warm-up iterations, then K timed iterations over the c2 train set (for K > 30 a uniform
+    sample of 30/K of the ratings, so the arm stays within a few minutes).  Falls back to the
+    oracle's threaded port of the batch-Hogwild update when mf-train could not be built."""
+    import tempfile
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from cumf_sgd_gb300 import synth
     t0 = time.time()
-    train, _ = synth.generate(synth.C2, seed=0, device="cuda" if _has_cuda() else "cpu")
+    train, test = synth.generate(synth.C2, seed=0, device="cuda" if _has_cuda() else "cpu")
     gen_s = time.time() - t0
-    per_step = []
-    budget = max(2.0, 60.0 / (args.warmup + args.steps))  # whole arm: about a minute of CPU work
-    for i in range(args.warmup + args.steps):
-        base = cpu_port_baseline(train, synth.C2.m, synth.C2.n, seconds_budget=budget)
-        if i >= args.warmup:
-            per_step.append(base)
-    v = statistics.mean(b["value"] for b in per_step)
-    line = {"impl": "reference", "metric": "sgd_updates_per_sec", "value": v, "unit": "updates/s",
+    threads = os.cpu_count() or 1
+    ref_tools = _reference_tools()
+    line = {"impl": "reference", "metric": "sgd_updates_per_sec", "unit": "updates/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "storage": "fp32 (CPU port)", "k": K},
-            "cpu_baseline": dict(per_step[-1], value=v),
-            "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "gen_seconds": gen_s}
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "gen_seconds": gen_s}
+    if ref_tools is not None:
+        frac = min(1.0, 30.0 / max(1, args.steps))
+        sample = train
+        if frac < 1.0:
+            keep = np.random.default_rng(0).random(len(train)) < frac
+            sample = train[keep]
+        with tempfile.TemporaryDirectory() as tmp:
+            base = libmf_baseline(ref_tools, sample, args.warmup + args.steps, threads, tmp,
+                                  warm_iters=args.warmup, test=test if frac == 1.0 else None)
+        v = base["value"]
+        line.update({"value": v, "ms_per_step": len(sample) / v * 1e3,
+                     "config": {"workload": WORKLOAD, "trainer": "LIBMF mf-train (test/mf-train.cpp)", "k": K,
+                                "threads": threads, "blocks": 2 * threads + 1, "l2": 0.05,
+                                "step": "one LIBMF iteration over the train set" +
+                                        ("" if frac == 1.0 else f" (uniform {frac:.3f} sample)")},
+                     "test_rmse": base.get("test_rmse_mf_predict"),
+                     "cpu_baseline": {**{k2: base[k2] for k2 in ("value", "unit", "cores", "kind", "build")},
+                                      "sample": f"{len(sample)} ratings x {args.steps} timed iterations "
+                                                f"(after {args.warmup} warm-up iterations), {threads} threads"}})
+    else:
+        per_step = []
+        budget = max(2.0, 60.0 / (args.warmup + args.steps))  # whole arm: about a minute of CPU work
+        for i in range(args.warmup + args.steps):
+            b = cpu_port_baseline(train, synth.C2.m, synth.C2.n, seconds_budget=budget)
+            if i >= args.warmup:
+                per_step.append(b)
+        v = statistics.mean(b["value"] for b in per_step)
+        line.update({"value": v, "config": {"workload": WORKLOAD, "storage": "fp32 (CPU port)", "k": K},
+                     "cpu_baseline": dict(per_step[-1], value=v),
+                     "note": "LIBMF mf-train not built on this host (no reference sources): oracle port timed"})
+    line["e2e"] = {"value": line["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     print(json.dumps(line), flush=True)
 
 
@@ -383,27 +447,36 @@ def run_warmstart_suite(args, quiet=False):
         return None, None
 
     # 4. cold start
-    _, _, crm, cms = solve(g_tr, m_all, n, seed=5, precision="fp16", iters=40, te=g_te)
+    _, _, crm, cms = solve(g_tr, m_all, n, seed=5, precision="fp16", iters=args.warm_max_epochs, te=g_te)
     cold_ms, cold_ep = time_to_target(crm, cms)
     out({"arm": "cold fp16", "epoch_rmse": [round(x, 5) for x in crm], "epoch_ms": [round(x, 3) for x in cms],
          "time_to_target_ms": cold_ms, "epochs_to_target": cold_ep})
 
-    def warm(use_mlp, precision, alpha, beta, tail_epochs):
+    def warm(init_kind, precision, alpha, beta, tail_epochs):
+        """init_kind: "mlp" (the learned encoder), or a non-learned start on the same deployed
+        base model: "qmean" (the encoder's own input, the rating-centred mean of the rated
+        items' factors), "zero" (rows of zeros: the first prediction is the global mean) or
+        "random" (the plain SGD initialisation)."""
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         P0 = torch.empty(m_all, K, device=dev)
         P0[: base_spec.m] = base_P
-        if use_mlp:  # features of the new users from their ratings (the tail of the array)
+        if init_kind in ("mlp", "qmean"):  # features of the new users (the tail of the array)
             tail = d_gtr[len(b_tr) * 12:].view(torch.int32).view(-1, 3).clone()
             tail[:, 0] -= base_spec.m  # the new users' own ids 0..new_users-1
             Xn = features(tail, len(n_tr), new_users, n, base_Q)
-            mlp.forward(Xn.data_ptr(), new_users, P0[base_spec.m:].data_ptr())
+            if init_kind == "mlp":
+                mlp.forward(Xn.data_ptr(), new_users, P0[base_spec.m:].data_ptr())
+            else:
+                P0[base_spec.m:] = Xn[:, :K]
+        elif init_kind == "zero":
+            P0[base_spec.m:] = 0
         else:
             P0[base_spec.m:] = torch.from_numpy(oracle.init_factors(new_users, K, "fp32", 9, 1)).to(dev)
         torch.cuda.synchronize()
         prep_ms = (time.perf_counter() - t0) * 1e3
         init = cm.DeviceModel(P0.data_ptr(), m_all, base_Q.data_ptr(), n, K)
-        _, _, wrm, wms = solve(g_tr, m_all, n, seed=5, precision=precision, iters=args.e2e_epochs, init=init,
+        _, _, wrm, wms = solve(g_tr, m_all, n, seed=5, precision=precision, iters=args.warm_max_epochs, init=init,
                                te=g_te, alpha=alpha, beta=beta, tail_epochs=tail_epochs, tail_start=len(b_tr))
         Pn = P0[base_spec.m:].contiguous()
         d_nte = torch.from_numpy((n_te.copy()).view(np.uint8)).to(dev)
@@ -414,13 +487,15 @@ def run_warmstart_suite(args, quiet=False):
         return prep_ms, wrm, wms, init_rmse_new
 
     configs = [c.split(":") for c in args.warm_configs.split(",")]
-    for use_mlp in (True, False):
-        for precision, alpha, beta, tail in (configs if use_mlp else configs[:1]):
-            prep_ms, wrm, wms, init_new = warm(use_mlp, precision, float(alpha), float(beta), int(tail))
+    labels = {"mlp": "", "qmean": " (no MLP: centred item-factor mean)", "zero": " (no MLP: zero rows)",
+              "random": " (no MLP: random rows)"}
+    for init_kind in ("mlp", "qmean", "zero", "random"):
+        for precision, alpha, beta, tail in (configs if init_kind == "mlp" else configs[:1]):
+            prep_ms, wrm, wms, init_new = warm(init_kind, precision, float(alpha), float(beta), int(tail))
             w_ms, w_ep = time_to_target(wrm, wms)
             total = None if w_ms is None else w_ms + prep_ms
-            out({"arm": f"warm {precision} alpha={alpha} beta={beta} new-user epochs={tail}" +
-                        ("" if use_mlp else " (no MLP: random new users)"), "mlp": use_mlp,
+            out({"arm": f"warm {precision} alpha={alpha} beta={beta} new-user epochs={tail}" + labels[init_kind],
+                 "init": init_kind, "mlp": init_kind == "mlp",
                  "prep_ms": prep_ms, "new_user_test_rmse_at_init": init_new,
                  "epoch_rmse": [round(x, 5) for x in wrm], "epoch_ms": [round(x, 3) for x in wms],
                  "time_to_target_ms": total, "epochs_to_target": w_ep,
@@ -429,25 +504,73 @@ def run_warmstart_suite(args, quiet=False):
             "cold_epochs": cold_ep, "arms": [r for r in results if "arm" in r and r["arm"] != "cold fp16"]}
 
 
-def warm_summary(args):
-    """Time-to-target line for bench.py's default run: c2 shape, cold fp16 against the MLP
-    warm start with bf16 stochastic rounding (one schedule) and its no-MLP ablation."""
+def warm_summary(args, scale=2.0):
+    """Time-to-target line for bench.py's default run (scale 2: the c2 shape; scale 1: the c1
+    shape): cold fp16 against the MLP warm start with bf16 stochastic rounding (one schedule),
+    and the same deployed base model and schedule without the MLP (centred item-factor mean,
+    zero rows, random rows), every arm capped at 40 epochs."""
     a = argparse.Namespace(**vars(args))
-    a.scale, a.mlp_epochs, a.e2e_epochs = 2.0, 10, 20
+    a.scale, a.e2e_epochs, a.warm_max_epochs = scale, 20, 40
+    a.mlp_epochs = 10 if scale >= 2.0 else 30
     a.warm_configs = "bf16sr:0.04:0.3:4"
     r = run_warmstart_suite(a, quiet=True)
-    warm = next(x for x in r["arms"] if x.get("mlp"))
-    abl = next((x for x in r["arms"] if not x.get("mlp")), None)
-    return {"shape": "c2 base 480189x17770 (99.07M ratings) + 50000 new users (+5% ratings), k=128",
+    warm = next(x for x in r["arms"] if x.get("init") == "mlp")
+    heur = {x["init"]: x for x in r["arms"] if x.get("init") != "mlp"}
+    reached = [x["time_to_target_ms"] for x in heur.values() if x["time_to_target_ms"]]
+    best_heur = min(reached) if reached else None
+    big = scale >= 2.0
+    return {"shape": ("c2 base 480189x17770 (99.07M ratings)" if big else "c1 base 10000x2000 (0.9M ratings)") +
+                     " + 50000 new users (+5% ratings), k=128",
             "target_rmse": r["target_rmse"], "target": "FP64 oracle (host threads) test RMSE + 0.002",
+            "fp64_oracle_rmse": r["fp64_oracle_rmse"],
             "cold_fp16_ms": r["cold_fp16_ms"], "cold_fp16_epochs": r["cold_epochs"],
             "warm_bf16sr_ms": warm["time_to_target_ms"], "warm_bf16sr_epochs": warm["epochs_to_target"],
             "warm_prep_ms": warm["prep_ms"], "warm_schedule": warm["arm"],
+            "warm_new_user_rmse_at_init": warm["new_user_test_rmse_at_init"],
             "speedup": warm["speedup_vs_cold"],
-            "no_mlp_ablation_ms": abl["time_to_target_ms"] if abl else None}
+            "no_mlp_arms": {k: {"time_to_target_ms": v["time_to_target_ms"], "epochs": v["epochs_to_target"],
+                                "new_user_rmse_at_init": v["new_user_test_rmse_at_init"]} for k, v in heur.items()},
+            "no_mlp_ablation_ms": best_heur,
+            "speedup_vs_heuristic": (best_heur / warm["time_to_target_ms"])
+            if (best_heur and warm["time_to_target_ms"]) else None,
+            "max_epochs": 40}
 
 
-def run_batched_suite(args):
+def batched_summary(args):
+    """Compact batched line for the default run: the 64-problem c4 set, 20 epochs, one
+    graph-captured persistent launch (autotuned) against 64 sequential plain launches per epoch."""
+    a = argparse.Namespace(**vars(args))
+    a.scale, a.e2e_epochs = 1.0, 20
+    return run_batched_suite(a, quiet=True)
+
+
+def precision_gap_summary(args):
+    """Every storage type's test-RMSE gap to the serial FP64 oracle on a c3-family problem
+    at 1% of the c3 size (10,009 x 6,249, 2.53M train ratings on 0..100, k=128, 20 epochs):
+    the same size as the c3 sweep's 1%-user sub-problem, small enough for the serial oracle."""
+    import cumf_sgd_gb300 as cm
+    from cumf_sgd_gb300 import synth
+    from oracle import oracle
+    oracle.build_oracle()
+    spec = synth.scaled(synth.C3, 0.01)
+    train, test = synth.generate(spec, seed=3, device="cuda")
+    sm, _, _ = cm.device_info(0)
+    W = cm.auto_workers(len(train), sm, K, "fp16")
+    t0 = time.time()
+    P, Q, b = oracle.train_f64(train, spec.m, spec.n, k=K, num_workers=W, num_iters=20, alpha=0.08, beta=0.3,
+                               seed=1)
+    ref = oracle.calc_rmse_f64(test, P, Q, b)
+    out = {"shape": f"c3 family at 1%: {spec.m}x{spec.n}, {len(train)} train / {len(test)} test ratings, k=128",
+           "workers": W, "epochs": 20, "fp64_oracle_rmse": ref, "fp64_oracle_secs": time.time() - t0, "gap": {}}
+    prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n)
+    tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+    for prec in ("fp32", "fp16", "bf16", "bf16sr", "fp16sr"):
+        par = cm.Parameter(k=K, num_workers=W, num_iters=20, alpha=0.08, beta=0.3, seed=1, gpu=0, precision=prec)
+        out["gap"][prec] = cm.calc_rmse(tprob, cm.sgd_train(prob, None, par)) - ref
+    return out
+
+
+def run_batched_suite(args, quiet=False):
     """Batched factorizations: 64 planted problems, users log-uniform in
     [1k, 200k], items in [500, 20k], ratings in [50k, 10M], k in {32, 64, 128}, planted rank
     in [8, 32], integer ratings 1..5, fp16 factors, 20 epochs.
@@ -488,8 +611,15 @@ def run_batched_suite(args):
         probs.append(dict(m=m, n=n, nnz=nnz, k=k, d_R=d_R, P=P, Q=Q, pm=pm, qm=qm, lr=lr, scale=scale,
                           b=float(np.float32(mean) / np.float32(std)), lam=float(np.float32(0.05) / scale),
                           te=torch.from_numpy(te.view(np.uint8)).to(dev), nte=len(te), seed=i))
-    print(json.dumps({"suite": "batched", "event": "generated", "problems": nprob,
-                      "total_nnz": sum(p["nnz"] for p in probs), "secs": time.time() - t0}), flush=True)
+    results = []
+
+    def emit(d):
+        results.append(d)
+        if not quiet:
+            print(json.dumps({"suite": "batched", **d}), flush=True)
+
+    emit({"event": "generated", "problems": nprob, "total_nnz": sum(p["nnz"] for p in probs),
+          "secs": time.time() - t0})
 
     def init_all():
         for p in probs:
@@ -523,9 +653,8 @@ def run_batched_suite(args):
     seq_ms = e0.elapsed_time(e1)
     seq_rmse = rmses()
     total = sum(p["nnz"] for p in probs)
-    print(json.dumps({"suite": "batched", "arm": "64 sequential plain launches per epoch", "epochs": epochs,
-                      "ms": seq_ms, "updates_per_sec": total * epochs / (seq_ms * 1e-3),
-                      "launches": epochs * nprob}), flush=True)
+    emit({"arm": "64 sequential plain launches per epoch", "epochs": epochs, "ms": seq_ms,
+          "updates_per_sec": total * epochs / (seq_ms * 1e-3), "launches": epochs * nprob})
     # batched persistent launch
     init_all()
     batch = cm.Batch([dict(d_R=p["d_R"].data_ptr(), nnz=p["nnz"], d_P=p["P"].data_ptr(), m=p["m"], n=p["n"],
@@ -545,14 +674,19 @@ def run_batched_suite(args):
     assert batch.status() == 0
     bat_rmse = rmses()
     info = batch.info()
-    print(json.dumps({"suite": "batched", "arm": "one graph-captured persistent launch", "epochs": epochs,
-                      "ms": bat_ms, "updates_per_sec": total * epochs / (bat_ms * 1e-3), "launches": 1,
-                      "tuning": best, "autotune_s": tune_s, "samples_per_epoch": info["samples_per_epoch"],
-                      "speedup_vs_sequential": seq_ms / bat_ms}), flush=True)
-    print(json.dumps({"suite": "batched", "event": "rmse", "sequential_mean": float(seq_rmse.mean()),
-                      "batched_mean": float(bat_rmse.mean()),
-                      "max_abs_diff": float(np.abs(seq_rmse - bat_rmse).max()),
-                      "per_problem": [[round(a, 4), round(b, 4)] for a, b in zip(seq_rmse, bat_rmse)]}), flush=True)
+    emit({"arm": "one graph-captured persistent launch", "epochs": epochs, "ms": bat_ms,
+          "updates_per_sec": total * epochs / (bat_ms * 1e-3), "launches": 1, "tuning": best,
+          "autotune_s": tune_s, "samples_per_epoch": info["samples_per_epoch"],
+          "speedup_vs_sequential": seq_ms / bat_ms})
+    emit({"event": "rmse", "sequential_mean": float(seq_rmse.mean()), "batched_mean": float(bat_rmse.mean()),
+          "max_abs_diff": float(np.abs(seq_rmse - bat_rmse).max()),
+          "per_problem": [[round(a, 4), round(b, 4)] for a, b in zip(seq_rmse, bat_rmse)]})
+    return {"problems": nprob, "total_nnz": total, "epochs": epochs, "sequential_ms": seq_ms,
+            "batched_graph_ms": bat_ms, "speedup_vs_sequential": seq_ms / bat_ms,
+            "batched_updates_per_sec": total * epochs / (bat_ms * 1e-3), "tuning": best, "autotune_s": tune_s,
+            "mean_test_rmse_sequential": float(seq_rmse.mean()), "mean_test_rmse_batched": float(bat_rmse.mean()),
+            "max_abs_rmse_diff": float(np.abs(seq_rmse - bat_rmse).max())}
+
 
 
 def run_gemm_suite(args):
@@ -788,9 +922,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the time-to-target measurement")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 oracle run (no RMSE gaps)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the c1 time-to-target, batched and precision-gap keys")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the workload size (tests only)")
     ap.add_argument("--mlp-epochs", type=int, default=30)
+    ap.add_argument("--warm-max-epochs", type=int, default=40, help="epoch cap of every warm-start arm")
     ap.add_argument("--warm-configs",
                     default="bf16sr:0.04:0.3:4,bf16sr:0.02:0.05:8,bf16sr:0.04:0.3:2,fp16:0.04:0.3:4,bf16sr:0.02:0.3:0",
                     help="warm-start refinements as storage:alpha:beta:new_user_epochs, comma separated")
@@ -919,17 +1057,107 @@ def main():
                "test_rmse": test_rmse}
         del model
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_port_baseline(train, m, n, seconds_budget=args.ref_seconds)
+    # The benchmark shape at the reference's recommended worker count (52 per SM,
+    # README.md:61) through the same C ABI: throughput and test RMSE beside the default's.
+    w52 = None
+    if not args.no_e2e and rank == 0 and world == 1:
+        W52 = 52 * sm
+        par52 = cm.Parameter(**{**par.__dict__, "num_workers": W52})
+        model52, st52 = cm.sgd_train(prob, None, par52, with_stats=True)
+        w52 = {"workers": W52, "updates_per_sec": st52.updates_per_sec, "train_ms": st52.train_ms,
+               "epochs": args.e2e_epochs, "test_rmse": cm.calc_rmse(tprob, model52),
+               "timing": "CUDA events around the epochs inside cumf_train"}
+        del model52
 
-    ttt = None
+    import tempfile
+    tmpdir = tempfile.mkdtemp(prefix="cumf_bench_")
+    ref_tools = _reference_tools() if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
+
+    # The reference's own GPU trainer (singleGPU/ built for sm_103a) at the same worker count:
+    # its printed update_per_sec (host clock() around its one persistent launch) and the test
+    # RMSE of the model it writes, scored by the same evaluator.
+    refk = None
+    if ref_tools is not None and w52 is not None and ref_tools.available("cumf_sgd_ref"):
+        try:
+            tr_path = os.path.join(tmpdir, "c2_train.bin")
+            ref_tools.write_records(train, tr_path)
+            mp = os.path.join(tmpdir, "ref_gpu.model")
+            out = ref_tools.run_reference_gpu(tr_path, mp, w52["workers"], args.e2e_epochs, gpu=local)
+            refk = {"binary": "singleGPU cumf_sgd, built unmodified for sm_103a (two-function __shfl shim)",
+                    "kernel": "sgd_k128_kernel_hogwild_warp32_lrate", "workers": w52["workers"],
+                    "epochs": args.e2e_epochs, "update_per_sec": out["update_per_sec"], "process_wall_s": out["wall_s"],
+                    "timing": "the binary's own update_per_sec: host clock() around its launch and sync"}
+            if out["rc"] == 0:
+                refk["test_rmse"] = cm.calc_rmse(tprob, cm.load_model(mp))
+                w52["rmse_minus_reference_kernel"] = w52["test_rmse"] - refk["test_rmse"]
+                w52["speedup_vs_reference_kernel"] = (w52["updates_per_sec"] / refk["update_per_sec"]
+                                                      if refk["update_per_sec"] else None)
+            else:
+                refk["error"] = out["tail"][-300:]
+            os.unlink(tr_path)
+        except Exception as e:  # reported, never fatal to the throughput line
+            refk = {"error": repr(e)[:300]}
+
+    # FP64 oracle (the same statistics, id maps and sample schedule; its batches on the host
+    # threads) for the RMSE gaps.
+    fp64 = None
+    if not args.no_e2e and rank == 0 and world == 1 and not args.no_fp64:
+        from oracle import oracle
+        oracle.build_oracle()
+        t0 = time.time()
+        P64, Q64, b64 = oracle.train_f64(train, m, n, k=K, num_workers=workers, num_iters=args.e2e_epochs,
+                                         seed=rank, threads=os.cpu_count() or 1)
+        fp64 = {"test_rmse": oracle.calc_rmse_f64(test, P64, Q64, b64), "host_threads": os.cpu_count() or 1,
+                "workers": workers, "secs": time.time() - t0}
+        del P64, Q64
+        e2e["rmse_gap_to_fp64"] = e2e["test_rmse"] - fp64["test_rmse"]
+        if w52 is not None:
+            w52["rmse_gap_to_fp64"] = w52["test_rmse"] - fp64["test_rmse"]
+        if refk is not None and "test_rmse" in refk:
+            refk["rmse_gap_to_fp64"] = refk["test_rmse"] - fp64["test_rmse"]
+
+    # CPU baseline: LIBMF mf-train (the reference's CPU trainer) on the host cores, a bounded
+    # sample of 8 iterations over the full train set; the oracle's threaded port beside it.
+    cpu = cpu_port = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_port = cpu_port_baseline(train, m, n, seconds_budget=args.ref_seconds)
+        if ref_tools is not None:
+            try:
+                threads = os.cpu_count() or 1
+                cpu = libmf_baseline(ref_tools, train, 8, threads, tmpdir)
+                cpu["sample"] = (f"LIBMF mf-train (test/mf-train.cpp), 8 iterations over the {nnz} c2 train "
+                                 f"ratings, k=128, {threads} threads, {2 * threads + 1} blocks "
+                                 f"({cpu.get('build', '')})")
+                cpu["gpu_e2e_ratio"] = e2e["value"] / cpu["value"] if e2e else None
+            except Exception as e:
+                cpu = dict(cpu_port, note="LIBMF failed: " + repr(e)[:200])
+        else:
+            cpu = dict(cpu_port, note="LIBMF mf-train not built on this host: oracle port timed")
+    import shutil
+    shutil.rmtree(tmpdir, ignore_errors=True)
+
+    ttt = ttt_c1 = batched = precision_gap = None
     if rank == 0 and world == 1 and not args.no_warm:
         del train, test
         try:
             ttt = warm_summary(args)
         except Exception as e:  # reported, never fatal to the throughput line
             ttt = {"error": repr(e)[:300]}
+    if rank == 0 and world == 1 and not args.no_extras:
+        torch.cuda.empty_cache()
+        for key, fn in (("c1", lambda: warm_summary(args, scale=1.0)), ("batched", lambda: batched_summary(args)),
+                        ("precision", lambda: precision_gap_summary(args))):
+            try:
+                res = fn()
+            except Exception as e:  # reported, never fatal to the throughput line
+                res = {"error": repr(e)[:300]}
+            if key == "c1":
+                ttt_c1 = res
+            elif key == "batched":
+                batched = res
+            else:
+                precision_gap = res
+            torch.cuda.empty_cache()
 
     if rank == 0:
         line = {"metric": "sgd_updates_per_sec", "value": updates_per_sec, "unit": "updates/s",
@@ -941,12 +1169,16 @@ def main():
                            "samples_per_epoch": samples_per_launch,
                            "l2": "inputs larger than L2 (ratings 1.19 GB)", "parallelism": f"replicas{world}"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(),
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "traffic": UPDATE_KERNEL_DRAM_BYTES_C2 if (prec == "fp16" and args.scale >= 1.0) else None,
+                             "traffic_source": UPDATE_KERNEL_DRAM_BYTES_SOURCE,
                              "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
                 "l2_roofline": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
                                 "peak_kind": "L2-resident copy (2 x 16 MB, 400 passes in one launch), measured in this run"},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu,
-                "time_to_target": ttt}
+                "cpu_port": cpu_port, "fp64_oracle": fp64, "value_w52": w52, "reference_kernel": refk,
+                "time_to_target": ttt, "time_to_target_c1": ttt_c1, "batched": batched,
+                "precision_gap": precision_gap}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -497,6 +497,7 @@ int mpr_auc_device(const cumf_node *d_R, int64_t nnz, int32_t prob_m, int32_t pr
 using namespace cumf;
 
 extern "C" int cumf_evaluate(const cumf_problem *te, const cumf_model *model, int criterion, double *out) {
+    TraceRange trace("evaluate (mf-predict criterion)");
     if (!te || !model || !out) return fail(CUMF_ERR_ARG, "evaluate: NULL argument");
     const bool ranking = criterion >= kRowMPR && criterion <= kColAUC;
     if (!(criterion == kRMSE || criterion == kMAE || criterion == kGKL || criterion == kLOGLOSS || criterion == kACC ||

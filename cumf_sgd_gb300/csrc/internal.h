@@ -8,9 +8,30 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "cumf_sgd.h"
 
 namespace cumf {
+
+// ---- tracing ---------------------------------------------------------------------------
+// An NVTX range around a pipeline stage (prep, epochs, export, evaluation, ...), visible in
+// Nsight Systems / Nsight Compute timelines; without a tool attached a push/pop is a no-op
+// call.  end() closes the range early; the destructor closes it on every return path.
+class TraceRange {
+  public:
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { end(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+    void end() {
+        if (open_) nvtxRangePop();
+        open_ = false;
+    }
+
+  private:
+    bool open_ = true;
+};
 
 // ---- error reporting ---------------------------------------------------------------
 void set_error(const std::string &msg);
@@ -76,6 +97,8 @@ cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32
 cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
                              const float *Q, int32_t n, int k, float b, int blocks,
                              double *d_part, double *d_sum, cudaStream_t s);
+// Loads launch_rmse_grid's kernels onto the current device without launching them.
+cudaError_t load_rmse_kernels();
 
 // Order-independent digest of `bytes` (a multiple of 4) at d into *d_out.
 cudaError_t launch_digest(const void *d, uint64_t bytes, unsigned long long *d_out, cudaStream_t s);

@@ -567,6 +567,7 @@ int cumf_mlp_set_params(void *mlp, const float *host, int64_t count) {
 }
 
 int cumf_mlp_forward(void *mlp, const float *d_X, int64_t rows, float *d_Y, void *stream) {
+    TraceRange trace("warm start: MLP inference");
     Mlp *mp = static_cast<Mlp *>(mlp);
     if (!mp || !d_X || !d_Y || rows < 0) return fail(CUMF_ERR_ARG, "mlp_forward: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
@@ -594,6 +595,7 @@ int cumf_mlp_loss_grad(void *mlp, const float *d_X, const float *d_T, int64_t ro
 
 int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, int epochs, int batch, float lr,
                    uint64_t seed, double *final_loss, void *stream) {
+    TraceRange trace("warm start: MLP training");
     Mlp *mp = static_cast<Mlp *>(mlp);
     if (!mp || !d_X || !d_T || rows <= 0 || epochs < 0 || batch <= 0)
         return fail(CUMF_ERR_ARG, "mlp_train: bad arguments");
@@ -715,6 +717,7 @@ int cumf_mlp_train(void *mlp, const float *d_X, const float *d_T, int64_t rows, 
 
 int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int32_t n, int k, int32_t m,
                        float *d_X, void *stream) {
+    TraceRange trace("warm start: user features");
     if (!d_Q || !d_X || m <= 0 || n <= 0 || k <= 0 || nnz < 0 || (nnz > 0 && !d_R))
         return fail(CUMF_ERR_ARG, "user_features: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;

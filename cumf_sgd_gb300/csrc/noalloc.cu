@@ -16,9 +16,15 @@
 //    its partial, the final pass writes the total), so nothing needs clearing between calls;
 //  - all calls share the one array: calls whose kernels overlap on the GPU (different
 //    streams, or different host threads) race on it and must be serialised by the caller;
-//  - the first call on a device, with that device current, looks up the array's device
-//    address (cudaGetSymbolAddress) and caches it; make that first call before any stream
-//    capture.
+//  - the first call on a device, with that device current, is its set-up: it looks up the
+//    array's device address (cudaGetSymbolAddress), caches it, and loads the evaluator
+//    kernels.  Under CUDA's lazy module loading (the default) loading device code allocates,
+//    so that first call must come where allocation is still possible (at start-up, say) and
+//    before any stream capture; a call with nnz = 0 does the set-up and nothing else;
+//  - the cached address belongs to the device's current context: after a cudaDeviceReset
+//    in the same process it is stale, so the entry point must not be used across a reset;
+//  - the result equals cumf_dev_rmse's within the rounding of the double sum (the two split
+//    the ratings into different blocks) and is the same bits from call to call.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -52,6 +58,8 @@ int scratch_for_current_device(double **out) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_rmse_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_rmse_scratch)");
+        e = load_rmse_kernels();
+        if (e != cudaSuccess) return cuda_fail(e, "loading the evaluator kernels");
         g_scratch_addr[dev] = static_cast<double *>(p);
     }
     *out = g_scratch_addr[dev];
@@ -73,12 +81,12 @@ extern "C" int cumf_dev_rmse_noalloc(const cumf_node *d_R, int64_t nnz, const fl
     if (nnz > max_nnz)
         return fail(CUMF_ERR_ARG, "dev_rmse_noalloc: " + std::to_string(nnz) +
                                       " ratings exceed the fixed scratch limit of " + std::to_string(max_nnz));
-    if (nnz == 0) {
+    double *scratch = nullptr;
+    if (int rc = scratch_for_current_device(&scratch)) return rc;
+    if (nnz == 0) {  // set-up only
         *out_rmse = 0;
         return CUMF_OK;
     }
-    double *scratch = nullptr;
-    if (int rc = scratch_for_current_device(&scratch)) return rc;
     const int blocks = (int)((nnz + kNoAllocRatingsPerBlock - 1) / kNoAllocRatingsPerBlock);
     cudaStream_t s = (cudaStream_t)stream;
     CUMF_CUDA(launch_rmse_grid(d_R, nnz, d_P, m, d_Q, n, k, b, blocks, scratch, scratch + kNoAllocMaxBlocks, s));

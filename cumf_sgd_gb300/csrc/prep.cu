@@ -299,6 +299,16 @@ cudaError_t launch_import(const float *src, const int32_t *map, int64_t rows, in
     return cudaGetLastError();
 }
 
+// Forces the (lazily loaded) evaluator kernels of launch_rmse_grid onto the current device
+// without launching them: CUDA's lazy module loading would otherwise load them, and allocate
+// for their code, at the first launch.
+cudaError_t load_rmse_kernels() {
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, rmse_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, sum_kernel);
+    return e;
+}
+
 cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, int32_t m,
                              const float *Q, int32_t n, int k, float b, int blocks,
                              double *d_part, double *d_sum, cudaStream_t s) {

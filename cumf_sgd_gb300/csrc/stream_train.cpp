@@ -177,6 +177,7 @@ void parallel_for(int64_t n, F f) {
 int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int lanes,
                  cumf_model *out, cumf_train_stats *st) {
     const double t0 = now_ms();
+    TraceRange trace_prep("cumf_train (streamed): prep (stats, shuffle, grid, scale, init)");
     const int64_t nnz = tr->nnz;
     const int32_t m = tr->m, n = tr->n;
     const int k = p.k;
@@ -308,6 +309,8 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
 
     const std::vector<std::vector<Step>> sched = block_schedule(p, pr.rng);
     const double t1 = now_ms();
+    trace_prep.end();
+    TraceRange trace_epochs("cumf_train (streamed): epochs (block copies + updates)");
     Tuning tu;
     tu.lanes = lanes;
     tu.prefetch = p.prefetch;
@@ -340,7 +343,9 @@ int stream_train(const cumf_problem *tr, const cumf_params &p, int workers, int 
     int status = 0;
     CUMF_CUDA(cudaMemcpy(&status, d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
     const double t2 = now_ms();
+    trace_epochs.end();
     if (status != 0) return fail(CUMF_ERR_RANGE, "a rating index was outside its block");
+    TraceRange trace_export("cumf_train (streamed): export");
 
     // Export on the host: widen, unscale, un-permute (transform_half + scale_model +
     // shuffle_model); the model may not fit the device in these modes.

@@ -828,6 +828,7 @@ extern "C" int cumf_dev_parse_text(const void *d_text, int64_t len, int64_t star
 }
 
 extern "C" int cumf_read_text_problem(const char *path, int header_lines, int pinned, cumf_problem *out) {
+    TraceRange trace("text parse: read text problem");
     if (!out || header_lines < 0) return fail(CUMF_ERR_ARG, "bad read_text_problem arguments");
     memset(out, 0, sizeof(*out));
     out->m = out->n = 1;
@@ -903,6 +904,7 @@ extern "C" int cumf_convert_text(const char *in_path, const char *out_path, int 
 
 extern "C" int cumf_parse_text_host(const char *text, int64_t len, int header_lines, cumf_node *out, int64_t cap,
                                     int64_t *n_records) {
+    TraceRange trace("text parse: host text, overlapped chunks");
     if (!n_records || len < 0 || (len > 0 && !text) || header_lines < 0 || cap < 0 || (out == nullptr && cap > 0))
         return fail(CUMF_ERR_ARG, "parse_text_host: bad arguments");
     const unsigned char *p = reinterpret_cast<const unsigned char *>(text);

@@ -97,7 +97,9 @@ typedef struct cumf_params {
     int32_t precision;     /* CUMF_FP16 ...                                              */
     int32_t lanes;         /* lanes cooperating on one rating: 0 = auto, else 4..32     */
     int32_t quiet;         /* 1 = no informational stdout                               */
-    int32_t epochs_per_launch; /* mode A: 0 = one launch for all epochs (reference)     */
+    int32_t epochs_per_launch; /* mode A: 0 = one launch per epoch (default); N > 0 = N
+                                * epochs per launch while every worker is resident (N >=
+                                * num_iters: one persistent launch, as sgd_kernel.cu:212-244) */
     int32_t verbose_epochs;    /* 1 = print one JSON line per epoch (needs a test set)  */
     int32_t prefetch;      /* L2 prefetch distance in records: -1 = tuned default, 0 = off */
     int32_t l2_hints;      /* L2 eviction hints: -1 = tuned default, 0 = off, 1 = on      */
@@ -315,8 +317,12 @@ int cumf_dev_rmse(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m
  * the library until exit), so nnz is limited to 134,217,728 ratings; larger calls return
  * CUMF_ERR_ARG.  All calls share that array: calls whose kernels overlap on the GPU race and
  * must be serialised by the caller.  The first call on each device (with that device
- * current) looks up the array's address; make it before any stream capture.  Same inputs
- * and output as cumf_dev_rmse. */
+ * current) is its set-up: it looks up the array's address and loads the evaluator kernels,
+ * which allocates under CUDA's lazy module loading; make it where allocation is still
+ * possible (at start-up) and before any stream capture.  A call with nnz = 0 does only that
+ * set-up.  Do not use it across a cudaDeviceReset (the cached address goes stale).  Same
+ * inputs as cumf_dev_rmse; the result equals cumf_dev_rmse's within the rounding of the
+ * double sum (different block split) and is identical from call to call. */
 int cumf_dev_rmse_noalloc(const cumf_node *d_R, int64_t nnz, const float *d_P, int32_t m,
                           const float *d_Q, int32_t n, int k, float b, double *out_rmse,
                           void *stream);

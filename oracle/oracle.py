@@ -39,19 +39,34 @@ def build_oracle() -> str:
 
 
 def build_reference() -> bool:
-    """Builds oracle/_ref from the reference tree when it is present; returns availability."""
+    """Builds oracle/_ref from the reference tree when it is present, or (on the GPU host,
+    which has no reference tree) the trainer tools from the sources ref_build.sh staged in
+    oracle/_ref/src; returns whether the reference trainers are available."""
     ref = os.environ.get("CUMF_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "test")):
-        return reference_available()
+    staged = os.path.isfile(os.path.join(REF_DIR, "src", "singleGPU", "sgd_kernel.cu"))
+    if not os.path.isdir(os.path.join(ref, "test")) and not staged:
+        return trainers_available()
     script = os.path.join(HERE, "ref_build.sh")
     res = subprocess.run(["bash", script], capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("reference build failed:\n" + res.stdout + res.stderr)
-    return reference_available()
+    return trainers_available()
 
 
 def reference_available() -> bool:
+    """The reference's host tools built on this machine (goldens: layouts, criteria)."""
     return all(os.access(os.path.join(REF_DIR, t), os.X_OK) for t in ("mf-predict", "ref_layout", "ref_rmse"))
+
+
+def trainers_available() -> bool:
+    """The reference's two trainers: LIBMF mf-train (CPU) and cumf_sgd_ref (the reference GPU
+    trainer, singleGPU/, built for sm_103a)."""
+    return all(os.access(os.path.join(REF_DIR, t), os.X_OK) for t in ("mf-train", "mf-predict", "cumf_sgd_ref"))
+
+
+def ref_build_info() -> str:
+    path = os.path.join(REF_DIR, "BUILD_INFO")
+    return open(path).read().strip() if os.path.exists(path) else ""
 
 
 class _SgdArgs(C.Structure):

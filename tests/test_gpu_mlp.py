@@ -1,6 +1,11 @@
-"""Warm-start MLP on the tensor cores against its FP64 CPU restatement (oracle/mlp_oracle.py).
-Tolerances: activations and backward operands are bf16, so loss within 1% and each
-gradient tensor within 3% (relative L2) of FP64; features within 1e-4 relative (fp32 atomics)."""
+"""Warm-start MLP on the tensor cores against its CPU restatements (oracle/mlp_oracle.py).
+Tolerances:
+  - against the restatement with the GPU's bf16 roundings (forward_backward_bf16): loss within
+    1e-3 and each gradient tensor within 3e-3 relative L2 (fp32 accumulation order and the odd
+    value rounded to the other bf16 neighbour are the only differences);
+  - against exact FP64: each gradient tensor within its own bound from gradient_bounds (twice
+    the bf16-rounded restatement's own distance from FP64, plus 2e-3), about 0.6-1.1%;
+  - features within 1e-4 relative (fp32 atomics)."""
 import numpy as np
 import pytest
 
@@ -29,9 +34,12 @@ def test_mlp_loss_and_gradients_match_fp64(lib, cuda, rows):
     grads = mlp.get(1)
     ref_loss, ref_grads = mlp_oracle.forward_backward(params, X, T, D_IN, H, D_OUT)
     assert abs(loss - ref_loss) <= 0.01 * ref_loss, (loss, ref_loss)
-    for name, g, r in zip(["W1", "b1", "W2", "b2", "W3", "b3"], split(grads), split(ref_grads)):
-        err = np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-12)
-        assert err <= 0.03, (name, err)
+    l16, g16, g64, bounds = mlp_oracle.gradient_bounds(params, X, T, D_IN, H, D_OUT)
+    assert abs(loss - l16) <= 1e-3 * l16, (loss, l16)
+    for name, g, r16, r64 in zip(mlp_oracle.GRAD_NAMES, split(grads), split(g16), split(g64)):
+        e16, e64 = mlp_oracle.rel_err(g, r16), mlp_oracle.rel_err(g, r64)
+        assert e16 <= 3e-3, (name, e16)
+        assert e64 <= bounds[name], (name, e64, bounds[name])
     Y = torch.empty(rows, D_OUT, device=cuda)
     mlp.forward(dX.data_ptr(), rows, Y.data_ptr())
     torch.cuda.synchronize()

@@ -24,15 +24,26 @@ def test_noalloc_rmse_matches_allocating_entry_point(lib, cuda):
     d_P = torch.from_numpy((rng.standard_normal((m, k)) * 0.2).astype(np.float32)).to(cuda)
     d_Q = torch.from_numpy((rng.standard_normal((n, k)) * 0.2).astype(np.float32)).to(cuda)
     b = 3.1
+    # set-up call (nnz = 0): loads the evaluator code while allocation is still allowed
+    zero = C.c_double(-1.0)
+    assert lib.cumf_dev_rmse_noalloc(None, 0, None, m, None, n, k, b, C.byref(zero), None) == 0
+    assert zero.value == 0.0
     ref = C.c_double()
     assert lib.cumf_dev_rmse(d_R.data_ptr(), nnz, d_P.data_ptr(), m, d_Q.data_ptr(), n, k, b,
                              C.byref(ref), None) == 0
-    for _ in range(2):  # the shared scratch keeps the last call's contents
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    first = None
+    for _ in range(3):  # the shared scratch keeps the last call's contents
         got = C.c_double()
         rc = lib.cumf_dev_rmse_noalloc(d_R.data_ptr(), nnz, d_P.data_ptr(), m, d_Q.data_ptr(), n, k, b,
                                        C.byref(got), None)
         assert rc == 0, lib.cumf_last_error()
         assert abs(got.value - ref.value) <= 1e-6 * ref.value, (got.value, ref.value)
+        first = got.value if first is None else first
+        assert got.value == first  # the same bits from call to call
+    # after the set-up call, evaluations take no device memory
+    assert torch.cuda.mem_get_info()[0] == free_before
     # a smaller second problem right after: stale partials of the bigger call must not leak in
     small = 10_000
     ref2, got2 = C.c_double(), C.c_double()
