@@ -565,8 +565,8 @@ class Batch:
         _lib.check(_lib.load().cumf_batch_create(arr, len(problems), C.byref(h)))
         self._h = h
 
-    def set_tuning(self, batches_target: int, order: int, blocks_per_sm: int) -> None:
-        t = _lib.BatchTuning(batches_target=batches_target, order=order, blocks_per_sm=blocks_per_sm)
+    def set_tuning(self, batches_target: int, order: int, blocks_per_sm: int, lanes: int = 16) -> None:
+        t = _lib.BatchTuning(batches_target=batches_target, order=order, blocks_per_sm=blocks_per_sm, lanes=lanes)
         _lib.check(_lib.load().cumf_batch_set_tuning(self._h, C.byref(t)))
 
     def info(self):
@@ -574,14 +574,14 @@ class Batch:
         tasks, samples = C.c_int(), C.c_int64()
         _lib.check(_lib.load().cumf_batch_get_info(self._h, C.byref(t), C.byref(tasks), C.byref(samples)))
         return dict(batches_target=t.batches_target, order=t.order, blocks_per_sm=t.blocks_per_sm,
-                    tasks_per_epoch=tasks.value, samples_per_epoch=samples.value)
+                    lanes=t.lanes, tasks_per_epoch=tasks.value, samples_per_epoch=samples.value)
 
     def autotune(self, stream: int = 0):
         t = _lib.BatchTuning()
         ms = C.c_double()
         _lib.check(_lib.load().cumf_batch_autotune(self._h, stream or None, C.byref(t), C.byref(ms)))
         return dict(batches_target=t.batches_target, order=t.order, blocks_per_sm=t.blocks_per_sm,
-                    epoch_ms=ms.value)
+                    lanes=t.lanes, epoch_ms=ms.value)
 
     def run(self, first_epoch: int, n_epochs: int, use_graph: bool = True, stream: int = 0) -> None:
         _lib.check(_lib.load().cumf_batch_run(self._h, first_epoch, n_epochs, int(use_graph), stream or None))

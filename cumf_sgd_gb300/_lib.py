@@ -82,7 +82,7 @@ class BatchProblem(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("batches_target", C.c_int32), ("order", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("reserved_", C.c_int32 * 5)]
+                ("lanes", C.c_int32), ("reserved_", C.c_int32 * 4)]
 
 
 class Args(C.Structure):

@@ -1,15 +1,15 @@
 // batch.cu - many independent factorizations in one persistent launch.
 //
 // Problems of uneven size (m, n, nnz) and factor length k in {32, 64, 128}, fp16 factors,
-// share one launch: a grid of resident blocks whose 16-lane worker groups take tasks from a
-// global counter.  A task is one Hogwild worker of one problem: it runs that worker's
+// share one launch: a grid of resident blocks whose G-lane worker groups (G = 8, 16 or 32,
+// chosen by the autotuner) take tasks from a global counter.  A task is one Hogwild worker of one problem: it runs that worker's
 // epochs of the launch in order, each its ceil(nnz/(W*128)) batches of 128 records exactly as
 // in sgd_update.cu, so a problem never has more than W workers in flight and there is no
 // barrier between epochs (as in the reference's persistent kernel).  The task table order is
-// chosen by the autotuner.  Each lane owns k/16 consecutive halves of a row (16, 8 or 4 B).
+// chosen by the autotuner.  Each lane owns k/G consecutive halves of a row (4 to 32 B).
 // The launch (counter reset + kernel) can be captured in a CUDA graph and replayed.
-// Autotuning times candidate schedules (workers per problem, task order, blocks per SM)
-// with an all-zero learning-rate table: the kernel then does the same loads and stores but
+// Autotuning times candidate schedules (lanes per worker, blocks per SM, workers per
+// problem, task order) with an all-zero learning-rate table: the kernel then does the same loads and stores but
 // writes back the values it read (p + 0 = p, exactly representable), so the factors are
 // left bit for bit unchanged.
 #include <cuda_fp16.h>
@@ -32,10 +32,7 @@ namespace cumf {
 namespace {
 
 constexpr int kBT = 256;       // threads per block
-constexpr int kBG = 16;        // lanes per worker
-constexpr int kBGPB = kBT / kBG;
-constexpr int kBChunk = 32;
-constexpr int kBWPL = kBChunk * 3 / kBG;
+constexpr int kBChunk = 32;    // records staged in shared memory at a time
 
 struct BatchProblemDev {
     const cumf_node *R;
@@ -56,19 +53,28 @@ struct BatchTask {
     int worker;
 };
 
+// A lane's slice of a row: E consecutive halves moved as NVEC vectors of type V.
 template <int E>
-struct HalfVec;
+struct LaneIO;
 template <>
-struct HalfVec<8> {
-    using T = uint4;
+struct LaneIO<2> {
+    using V = uint32_t;
+    static constexpr int NVEC = 1;
 };
 template <>
-struct HalfVec<4> {
-    using T = uint2;
+struct LaneIO<4> {
+    using V = uint2;
+    static constexpr int NVEC = 1;
 };
 template <>
-struct HalfVec<2> {
-    using T = uint32_t;
+struct LaneIO<8> {
+    using V = uint4;
+    static constexpr int NVEC = 1;
+};
+template <>
+struct LaneIO<16> {
+    using V = uint4;
+    static constexpr int NVEC = 2;
 };
 
 template <typename T>
@@ -81,14 +87,21 @@ __device__ __forceinline__ void bcp_async4(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-// One worker's epoch on one problem (16 lanes, E halves per lane).
-template <int E>
+// One worker's epoch on one problem: G lanes, E = k / G halves per lane (the lane's slice
+// starts at element lane * E).  Dot product: lane partial in element order, then a shfl.xor
+// butterfly over the G lanes (the order the oracle replays with lanes = G).
+template <int G, int E>
 __device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane, unsigned gmask,
                          uint32_t (*s_rec)[3][kBChunk + 1], int *bad) {
-    using V = typename HalfVec<E>::T;
-    constexpr int W = E / 2;  // 32-bit words (half pairs) per lane
-    V *const P = reinterpret_cast<V *>(pr.P) + lane;
-    V *const Q = reinterpret_cast<V *>(pr.Q) + lane;
+    using IO = LaneIO<E>;
+    using V = typename IO::V;
+    constexpr int NVEC = IO::NVEC;
+    constexpr int WPV = (int)(sizeof(V) / 4);  // 32-bit words (half pairs) per vector
+    constexpr int ROWV = G * NVEC;             // vectors per row
+    constexpr int WPL = kBChunk * 3 / G;       // staged record words per lane
+    static_assert((kBChunk * 3) % G == 0, "record staging must split over the lanes");
+    V *const P = reinterpret_cast<V *>(pr.P) + lane * NVEC;
+    V *const Q = reinterpret_cast<V *>(pr.Q) + lane * NVEC;
     const uint32_t *const Rw = reinterpret_cast<const uint32_t *>(pr.R);
     const uint64_t nnz = pr.nnz;
     const float lr = __ldg(pr.lr + ep);
@@ -98,21 +111,26 @@ __device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane
         uint64_t base = start + (uint64_t)((t % (128 / kBChunk)) * kBChunk);
         while (base >= nnz) base -= nnz;
 #pragma unroll
-        for (int i = 0; i < kBWPL; ++i) {
-            const int w = lane + i * kBG;
+        for (int i = 0; i < WPL; ++i) {
+            const int w = lane + i * G;
             uint64_t rec = base + (uint64_t)(w / 3);
             while (rec >= nnz) rec -= nnz;
             bcp_async4(&s_rec[buf][w % 3][w / 3], Rw + rec * 3 + (w % 3));
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
+    auto load = [&](V (&dst)[NVEC], V *base, uint32_t row, bool ok) {
+#pragma unroll
+        for (int i = 0; i < NVEC; ++i) dst[i] = ok ? __ldcg(base + (uint64_t)row * ROWV + i) : V{};
+    };
     fetch(0, 0);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncwarp(gmask);
     uint32_t u = s_rec[0][0][0], v = s_rec[0][1][0];
     bool ok = (u < pr.m) & (v < pr.n);
-    V fp = ok ? __ldcg(P + (uint64_t)u * kBG) : V{};
-    V fq = ok ? __ldcg(Q + (uint64_t)v * kBG) : V{};
+    V fp[NVEC], fq[NVEC];
+    load(fp, P, u, ok);
+    load(fq, Q, v, ok);
     for (int t = 0; t < chunks; ++t) {
         const int buf = t & 1;
         const bool has_next = t + 1 < chunks;
@@ -130,43 +148,58 @@ __device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane
                 vn = s_rec[buf ^ 1][1][0];
             }
             const bool okn = (un < pr.m) & (vn < pr.n);
-            V np = okn ? __ldcg(P + (uint64_t)un * kBG) : V{};
-            V nq = okn ? __ldcg(Q + (uint64_t)vn * kBG) : V{};
+            V np[NVEC], nq[NVEC];
+            load(np, P, un, okn);
+            load(nq, Q, vn, okn);
             if (ok) {
                 const float r = __uint_as_float(s_rec[buf][2][j]);
                 float s = 0.f;
 #pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp, w)));
-                    const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq, w)));
-                    s = __fmaf_rn(pp.x, qq.x, s);
-                    s = __fmaf_rn(pp.y, qq.y, s);
-                }
+                for (int i = 0; i < NVEC; ++i)
 #pragma unroll
-                for (int o = kBG / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                    for (int w = 0; w < WPV; ++w) {
+                        const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp[i], w)));
+                        const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq[i], w)));
+                        s = __fmaf_rn(pp.x, qq.x, s);
+                        s = __fmaf_rn(pp.y, qq.y, s);
+                    }
+#pragma unroll
+                for (int o = G / 2; o >= 1; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
                 const float err = r - s;
-                V wp, wq;
+                V wp[NVEC], wq[NVEC];
 #pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp, w)));
-                    const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq, w)));
-                    const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(pr.lp, pp.x)), pp.x);
-                    const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(pr.lp, pp.y)), pp.y);
-                    const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(pr.lq, qq.x)), qq.x);
-                    const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(pr.lq, qq.y)), qq.y);
-                    __half2 hp = __floats2half2_rn(px, py), hq = __floats2half2_rn(qx, qy);
-                    word(wp, w) = *reinterpret_cast<uint32_t *>(&hp);
-                    word(wq, w) = *reinterpret_cast<uint32_t *>(&hq);
+                for (int i = 0; i < NVEC; ++i)
+#pragma unroll
+                    for (int w = 0; w < WPV; ++w) {
+                        const float2 pp = __half22float2(*reinterpret_cast<__half2 *>(&word(fp[i], w)));
+                        const float2 qq = __half22float2(*reinterpret_cast<__half2 *>(&word(fq[i], w)));
+                        const float px = __fmaf_rn(lr, __fmaf_rn(err, qq.x, -__fmul_rn(pr.lp, pp.x)), pp.x);
+                        const float py = __fmaf_rn(lr, __fmaf_rn(err, qq.y, -__fmul_rn(pr.lp, pp.y)), pp.y);
+                        const float qx = __fmaf_rn(lr, __fmaf_rn(err, pp.x, -__fmul_rn(pr.lq, qq.x)), qq.x);
+                        const float qy = __fmaf_rn(lr, __fmaf_rn(err, pp.y, -__fmul_rn(pr.lq, qq.y)), qq.y);
+                        __half2 hp = __floats2half2_rn(px, py), hq = __floats2half2_rn(qx, qy);
+                        word(wp[i], w) = *reinterpret_cast<uint32_t *>(&hp);
+                        word(wq[i], w) = *reinterpret_cast<uint32_t *>(&hq);
+                    }
+#pragma unroll
+                for (int i = 0; i < NVEC; ++i) {
+                    __stcg(P + (uint64_t)u * ROWV + i, wp[i]);
+                    __stcg(Q + (uint64_t)v * ROWV + i, wq[i]);
                 }
-                __stcg(P + (uint64_t)u * kBG, wp);
-                __stcg(Q + (uint64_t)v * kBG, wq);
-                if (un == u) np = wp;
-                if (vn == v) nq = wq;
+                if (un == u)
+#pragma unroll
+                    for (int i = 0; i < NVEC; ++i) np[i] = wp[i];
+                if (vn == v)
+#pragma unroll
+                    for (int i = 0; i < NVEC; ++i) nq[i] = wq[i];
             } else {
                 *bad = 1;
             }
-            fp = np;
-            fq = nq;
+#pragma unroll
+            for (int i = 0; i < NVEC; ++i) {
+                fp[i] = np[i];
+                fq[i] = nq[i];
+            }
             u = un;
             v = vn;
             ok = okn;
@@ -175,14 +208,18 @@ __device__ void run_task(const BatchProblemDev &pr, int worker, int ep, int lane
     }
 }
 
+// Persistent grid; each G-lane group takes tasks from the global counter.  G is the lanes
+// per worker (8, 16 or 32; 32 needs every k >= 64).
+template <int G>
 __global__ void __launch_bounds__(kBT, 4)
 batch_kernel(const BatchProblemDev *probs, const BatchTask *tasks, int tasks_per_epoch, int first_epoch, int n_epochs,
              int *counter, int *status) {
-    __shared__ uint32_t s_rec[kBGPB][2][3][kBChunk + 1];
-    const int lane = threadIdx.x % kBG;
-    const int gib = threadIdx.x / kBG;
-    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(kBG - 1));
-    const int leader = (threadIdx.x & 31) & ~(kBG - 1);
+    constexpr int GPB = kBT / G;
+    __shared__ uint32_t s_rec[GPB][2][3][kBChunk + 1];
+    const int lane = threadIdx.x % G;
+    const int gib = threadIdx.x / G;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    const int leader = (threadIdx.x & 31) & ~(G - 1);
     int bad = 0;
     while (true) {
         int g = 0;
@@ -193,12 +230,15 @@ batch_kernel(const BatchProblemDev *probs, const BatchTask *tasks, int tasks_per
         const BatchProblemDev pr = probs[t.problem];
         if (pr.nnz == 0 || pr.batches == 0) continue;
         for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
-            switch (pr.k) {
-                case 128: run_task<8>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-                case 64: run_task<4>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-                case 32: run_task<2>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad); break;
-                default: bad = 1; break;
-            }
+            if (pr.k == 128 && G == 8) run_task<G, 16>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad);
+            else if ((pr.k == 128 && G == 16) || (pr.k == 64 && G == 8))
+                run_task<G, 8>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad);
+            else if ((pr.k == 128 && G == 32) || (pr.k == 64 && G == 16) || (pr.k == 32 && G == 8))
+                run_task<G, 4>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad);
+            else if ((pr.k == 64 && G == 32) || (pr.k == 32 && G == 16))
+                run_task<G, 2>(pr, t.worker, ep, lane, gmask, s_rec[gib], &bad);
+            else
+                bad = 1;
         }
     }
     if (bad && status && lane == 0) atomicExch(status, (int)CUMF_ERR_RANGE);
@@ -295,14 +335,34 @@ int batch_plan(Batch *b) {
     return CUMF_OK;
 }
 
+// Lanes per worker that every problem of the batch supports (k / lanes halves per lane, 2..16).
+bool lanes_fit(const Batch *b, int lanes) {
+    if (lanes != 8 && lanes != 16 && lanes != 32) return false;
+    for (const cumf_batch_problem &p : b->probs)
+        if (p.k / lanes < 2) return false;
+    return true;
+}
+
 cudaError_t batch_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     const int bps = std::max(1, std::min(4, b->tuning.blocks_per_sm));
-    batch_kernel<<<bps * b->sm_count, kBT, 0, s>>>(
-        zero_lr ? b->d_probs_zero_lr.as<BatchProblemDev>() : b->d_probs.as<BatchProblemDev>(),
-        b->d_tasks.as<BatchTask>(), b->tasks_per_epoch, first_epoch, n_epochs, b->d_counter.as<int>(),
-        b->d_status.as<int>());
+    const BatchProblemDev *probs = zero_lr ? b->d_probs_zero_lr.as<BatchProblemDev>() : b->d_probs.as<BatchProblemDev>();
+    const int grid = bps * b->sm_count;
+    switch (b->tuning.lanes) {
+        case 8:
+            batch_kernel<8><<<grid, kBT, 0, s>>>(probs, b->d_tasks.as<BatchTask>(), b->tasks_per_epoch, first_epoch,
+                                                  n_epochs, b->d_counter.as<int>(), b->d_status.as<int>());
+            break;
+        case 32:
+            batch_kernel<32><<<grid, kBT, 0, s>>>(probs, b->d_tasks.as<BatchTask>(), b->tasks_per_epoch, first_epoch,
+                                                   n_epochs, b->d_counter.as<int>(), b->d_status.as<int>());
+            break;
+        default:
+            batch_kernel<16><<<grid, kBT, 0, s>>>(probs, b->d_tasks.as<BatchTask>(), b->tasks_per_epoch, first_epoch,
+                                                   n_epochs, b->d_counter.as<int>(), b->d_status.as<int>());
+            break;
+    }
     return cudaGetLastError();
 }
 
@@ -332,6 +392,7 @@ int cumf_batch_create(const cumf_batch_problem *probs, int count, void **handle)
     b->tuning.batches_target = 16;
     b->tuning.order = 2;
     b->tuning.blocks_per_sm = 4;
+    b->tuning.lanes = 16;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
@@ -360,7 +421,11 @@ int cumf_batch_set_tuning(void *handle, const cumf_batch_tuning *t) {
     if (!b || !t || t->order < 0 || t->order > 2 || t->batches_target < 1 || t->blocks_per_sm < 1 ||
         t->blocks_per_sm > 4)
         return fail(CUMF_ERR_ARG, "batch_set_tuning: bad tuning");
-    b->tuning = *t;
+    cumf_batch_tuning c = *t;
+    if (c.lanes == 0) c.lanes = 16;
+    if (!lanes_fit(b, c.lanes))
+        return fail(CUMF_ERR_ARG, "batch_set_tuning: lanes must be 8, 16 or 32 (32 needs every k >= 64)");
+    b->tuning = c;
     return batch_plan(b);
 }
 
@@ -419,34 +484,50 @@ int cumf_batch_autotune(void *handle, void *stream, cumf_batch_tuning *best, dou
     Event e0, e1;
     CUMF_CUDA(e0.create());
     CUMF_CUDA(e1.create());
-    cumf_batch_tuning cand, top = b->tuning;
+    cumf_batch_tuning top = b->tuning;
     double top_ms = 1e30;
-    memset(&cand, 0, sizeof(cand));
+    // Time per sample of one epoch with a zero learning rate (factors unchanged), so schedules
+    // with different budgets compare fairly.
+    auto trial = [&](const cumf_batch_tuning &cand) -> int {
+        b->tuning = cand;
+        if (int rc = batch_plan(b)) return rc;
+        CUMF_CUDA(batch_launch(b, true, 0, 1, s));  // warm-up
+        CUMF_CUDA(cudaEventRecord(e0.e, s));
+        CUMF_CUDA(batch_launch(b, true, 0, 1, s));
+        CUMF_CUDA(cudaEventRecord(e1.e, s));
+        CUMF_CUDA(cudaEventSynchronize(e1.e));
+        float ms = 0;
+        CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
+        const double per = ms / (double)std::max<int64_t>(1, b->samples_per_epoch);
+        if (per < top_ms) {
+            top_ms = per;
+            top = cand;
+        }
+        return CUMF_OK;
+    };
+    // Stage 1: lanes per worker x blocks per SM at the default budget and order; stage 2:
+    // budget x task order at the chosen lanes and blocks.
+    const int lanes_c[] = {8, 16, 32};
+    const int occ[] = {3, 4};
     const int targets[] = {4, 8, 16, 32};
     const int orders[] = {0, 1, 2};
-    const int occ[] = {3, 4};
+    cumf_batch_tuning cand = top;
+    for (int g : lanes_c) {
+        if (!lanes_fit(b, g)) continue;
+        for (int bps : occ) {
+            cand.lanes = g;
+            cand.blocks_per_sm = bps;
+            if (int rc = trial(cand)) return rc;
+        }
+    }
+    const cumf_batch_tuning stage1 = top;
     for (int bt : targets)
-        for (int o : orders)
-            for (int bps : occ) {
-                cand.batches_target = bt;
-                cand.order = o;
-                cand.blocks_per_sm = bps;
-                b->tuning = cand;
-                if (int rc = batch_plan(b)) return rc;
-                CUMF_CUDA(batch_launch(b, true, 0, 1, s));  // warm-up, zero learning rate
-                CUMF_CUDA(cudaEventRecord(e0.e, s));
-                CUMF_CUDA(batch_launch(b, true, 0, 1, s));
-                CUMF_CUDA(cudaEventRecord(e1.e, s));
-                CUMF_CUDA(cudaEventSynchronize(e1.e));
-                float ms = 0;
-                CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
-                // time per sample, so schedules with different budgets compare fairly
-                const double per = ms / (double)std::max<int64_t>(1, b->samples_per_epoch);
-                if (per < top_ms) {
-                    top_ms = per;
-                    top = cand;
-                }
-            }
+        for (int o : orders) {
+            cand = stage1;
+            cand.batches_target = bt;
+            cand.order = o;
+            if (int rc = trial(cand)) return rc;
+        }
     b->tuning = top;
     if (int rc = batch_plan(b)) return rc;
     if (best) *best = top;

@@ -467,12 +467,14 @@ typedef struct cumf_batch_problem {
 /* Schedule of a batched launch: workers per problem so each has about batches_target
  * 128-record batches per epoch (problems with num_workers > 0 keep theirs); task order
  * 0 = problem by problem, 1 = round robin over problems, 2 = largest problems first;
- * blocks_per_sm 1..4 of the persistent grid. */
+ * blocks_per_sm 1..4 of the persistent grid; lanes per worker 8, 16 or 32 (0 = 16; 32 needs
+ * every problem's k >= 64), each lane moving k / lanes consecutive halves of a row. */
 typedef struct cumf_batch_tuning {
     int32_t batches_target;
     int32_t order;
     int32_t blocks_per_sm;
-    int32_t reserved_[5];
+    int32_t lanes;
+    int32_t reserved_[4];
 } cumf_batch_tuning;
 
 /* Copies the problem descriptors (the device buffers stay the caller's). */
@@ -486,8 +488,9 @@ int cumf_batch_get_info(void *batch, cumf_batch_tuning *tuning, int *tasks_per_e
 int cumf_batch_run(void *batch, int first_epoch, int n_epochs, int use_graph, void *stream);
 /* CUMF_ERR_RANGE if any launch met an out-of-range index (such ratings are skipped). */
 int cumf_batch_status(void *batch, int *status);
-/* Times every candidate schedule for one epoch with a zero learning rate (factors are left
- * bit for bit unchanged), keeps the fastest per sample and returns it. */
+/* Autotuner: times candidate schedules for one epoch each with a zero learning rate (factors
+ * are left bit for bit unchanged) and keeps the fastest per sample: first lanes per worker
+ * (8/16/32) x blocks per SM (3/4), then batch budget (4/8/16/32) x task order (0/1/2). */
 int cumf_batch_autotune(void *batch, void *stream, cumf_batch_tuning *best, double *best_epoch_ms);
 
 #ifdef __cplusplus

@@ -1,5 +1,6 @@
 """Batched persistent launch of many factorizations against the oracle (one worker per
-problem: bit-exact), its autotuner (zero learning rate: factors unchanged) and graph replay."""
+problem: bit-exact at every lane width), its autotuner (zero learning rate: factors
+unchanged; lane widths a problem's k cannot take are refused) and graph replay."""
 import numpy as np
 import pytest
 
@@ -10,14 +11,14 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(60, 30, 900, 32), (45, 70, 2000, 64), (80, 40, 3100, 128), (7, 5, 100, 128), (33, 21, 129, 64)]
 
 
-def make(cuda, seed, workers=1, lr_len=8):
+def make(cuda, seed, workers=1, lr_len=8, min_k=0):
     import torch
     from oracle import oracle
     rng = np.random.default_rng(seed)
     probs, host = [], []
     lr = oracle.lr_table(0.08, 0.3, 0.0, lr_len)
     d_lr = torch.from_numpy(lr).to(cuda)
-    for i, (m, n, nnz, k) in enumerate(SHAPES):
+    for i, (m, n, nnz, k) in enumerate(s for s in SHAPES if s[3] >= min_k):
         rec = np.empty(nnz, dtype=cm.NODE_DTYPE)
         rec["u"], rec["v"] = rng.integers(0, m, nnz), rng.integers(0, n, nnz)
         rec["r"] = rng.integers(1, 6, nnz).astype(np.float32) / np.float32(1.3)
@@ -38,10 +39,14 @@ def as_f32(t, rows, k):
     return t.view(torch.float16).reshape(rows, k).float().cpu().numpy()
 
 
-def test_batched_single_worker_bit_exact(lib, orc, cuda):
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_batched_single_worker_bit_exact(lib, orc, cuda, lanes):
+    """Each lane width the autotuner can pick (32 lanes only for k >= 64)."""
     import torch
-    probs, host, lr, _keep = make(cuda, 1)
+    probs, host, lr, _keep = make(cuda, 1, min_k=64 if lanes == 32 else 0)
     b = cm.Batch(probs)
+    b.set_tuning(16, 2, 4, lanes=lanes)
+    assert b.info()["lanes"] == lanes
     for ep in range(2):
         b.run(ep, 1, use_graph=(ep == 1))
     torch.cuda.synchronize()
@@ -49,7 +54,7 @@ def test_batched_single_worker_bit_exact(lib, orc, cuda):
     for h in host:
         P = orc.init_factors(h["m"], h["k"], "fp16", h["seed"], 1)
         Q = orc.init_factors(h["n"], h["k"], "fp16", h["seed"], 2)
-        orc.sgd_epochs(h["rec"], P, Q, "fp16", 1, lr, 0, 2, 0.05, 0.04, h["seed"], lanes=16)
+        orc.sgd_epochs(h["rec"], P, Q, "fp16", 1, lr, 0, 2, 0.05, 0.04, h["seed"], lanes=lanes)
         np.testing.assert_array_equal(as_f32(h["P"], h["m"], h["k"]), P)
         np.testing.assert_array_equal(as_f32(h["Q"], h["n"], h["k"]), Q)
 
@@ -62,6 +67,7 @@ def test_autotune_leaves_factors_unchanged_and_graph_matches_direct(lib, cuda):
     best = b.autotune()
     torch.cuda.synchronize()
     assert best["epoch_ms"] > 0 and best["order"] in (0, 1, 2)
+    assert best["lanes"] in (8, 16)  # a k = 32 problem rules out 32 lanes
     for h, (p0, q0) in zip(host, before):
         assert torch.equal(h["P"], p0) and torch.equal(h["Q"], q0)
     # one worker per problem: the graph replay and a direct launch give the same bits
@@ -115,3 +121,14 @@ def test_batched_hogwild_matches_plain_kernel_quality(lib, cuda):
         runs[arm] = out
     for a, b_ in zip(runs["plain"], runs["batched"]):
         assert abs(a - b_) <= 0.05 * a, runs
+
+
+def test_batched_tuning_refuses_lanes_a_problem_cannot_take(lib, cuda):
+    from cumf_sgd_gb300 import _lib
+    probs, host, _, _keep = make(cuda, 4)  # includes k = 32: 32 lanes would give one half per lane
+    b = cm.Batch(probs)
+    with pytest.raises(RuntimeError):
+        b.set_tuning(16, 2, 4, lanes=32)
+    with pytest.raises(RuntimeError):
+        b.set_tuning(16, 2, 4, lanes=12)
+    assert b.info()["lanes"] == 16
