@@ -454,9 +454,11 @@ def run_warmstart_suite(args, quiet=False):
 
     def warm(init_kind, precision, alpha, beta, tail_epochs):
         """init_kind: "mlp" (the learned encoder), or a non-learned start on the same deployed
-        base model: "qmean" (the encoder's own input, the rating-centred mean of the rated
-        items' factors), "zero" (rows of zeros: the first prediction is the global mean) or
-        "random" (the plain SGD initialisation)."""
+        base model: "mean" (the mean of the rated items' factors, scaled so that its product
+        with that mean is the user's mean rating), "qmean" (the encoder's own input, the
+        rating-centred mean of the rated items' factors), "zero" (rows of zeros; the model
+        has no bias term, so every first prediction is 0) or "random" (the plain SGD
+        initialisation)."""
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         P0 = torch.empty(m_all, K, device=dev)
@@ -469,6 +471,16 @@ def run_warmstart_suite(args, quiet=False):
                 mlp.forward(Xn.data_ptr(), new_users, P0[base_spec.m:].data_ptr())
             else:
                 P0[base_spec.m:] = Xn[:, :K]
+        elif init_kind == "mean":  # p = mean_u * qbar_u / |qbar_u|^2, so p . qbar_u = the user's mean rating
+            tail = d_gtr[len(b_tr) * 12:].view(torch.int32).view(-1, 3)
+            uu = (tail[:, 0] - base_spec.m).long()
+            vv = tail[:, 1].long()
+            rr = tail[:, 2].view(torch.float32)
+            deg = torch.zeros(new_users, device=dev).index_add_(0, uu, torch.ones_like(rr)).clamp_(min=1)
+            mu = torch.zeros(new_users, device=dev).index_add_(0, uu, rr) / deg
+            avg = torch.sparse_coo_tensor(torch.stack([uu, vv]), 1.0 / deg[uu], (new_users, n))
+            qbar = torch.sparse.mm(avg, base_Q)  # mean of each new user's rated item rows
+            P0[base_spec.m:] = qbar * (mu / (qbar * qbar).sum(1).clamp_(min=1e-12))[:, None]
         elif init_kind == "zero":
             P0[base_spec.m:] = 0
         else:
@@ -487,9 +499,10 @@ def run_warmstart_suite(args, quiet=False):
         return prep_ms, wrm, wms, init_rmse_new
 
     configs = [c.split(":") for c in args.warm_configs.split(",")]
-    labels = {"mlp": "", "qmean": " (no MLP: centred item-factor mean)", "zero": " (no MLP: zero rows)",
+    labels = {"mlp": "", "mean": " (no MLP: item-factor mean scaled to the user's mean rating)",
+              "qmean": " (no MLP: centred item-factor mean)", "zero": " (no MLP: zero rows)",
               "random": " (no MLP: random rows)"}
-    for init_kind in ("mlp", "qmean", "zero", "random"):
+    for init_kind in ("mlp", "mean", "qmean", "zero", "random"):
         for precision, alpha, beta, tail in (configs if init_kind == "mlp" else configs[:1]):
             prep_ms, wrm, wms, init_new = warm(init_kind, precision, float(alpha), float(beta), int(tail))
             w_ms, w_ep = time_to_target(wrm, wms)
@@ -545,14 +558,21 @@ def batched_summary(args):
 
 
 def precision_gap_summary(args):
-    """Every storage type's test-RMSE gap to the serial FP64 oracle on a c3-family problem
-    at 1% of the c3 size (10,009 x 6,249, 2.53M train ratings on 0..100, k=128, 20 epochs):
-    the same size as the c3 sweep's 1%-user sub-problem, small enough for the serial oracle."""
+    """Every storage type's test-RMSE gap to the serial FP64 oracle on the sub-problem the
+    c3 sweep measures it on: 1% of the c3 users with all 624,961 items (10,009 users, 2.53M
+    train / 40k test ratings on 0..100, the c3 family's Zipf exponents, rank 48 + N(0, 20)
+    noise), k=128, 20 epochs, generated directly at that size; every GPU variant and the
+    oracle use the same worker count."""
+    import dataclasses
     import cumf_sgd_gb300 as cm
     from cumf_sgd_gb300 import synth
     from oracle import oracle
     oracle.build_oracle()
-    spec = synth.scaled(synth.C3, 0.01)
+    c3 = synth.C3
+    total = c3.nnz_train + c3.nnz_test
+    spec = dataclasses.replace(c3, m=c3.m // 100, nnz_train=c3.nnz_train // 100, nnz_test=c3.nnz_test // 100,
+                               user_s=c3.user_s if c3.user_s >= 0 else synth.fit_zipf_exponent(c3.m, total, c3.top_user),
+                               item_s=c3.item_s if c3.item_s >= 0 else synth.fit_zipf_exponent(c3.n, total, c3.top_item))
     train, test = synth.generate(spec, seed=3, device="cuda")
     sm, _, _ = cm.device_info(0)
     W = cm.auto_workers(len(train), sm, K, "fp16")
@@ -560,7 +580,8 @@ def precision_gap_summary(args):
     P, Q, b = oracle.train_f64(train, spec.m, spec.n, k=K, num_workers=W, num_iters=20, alpha=0.08, beta=0.3,
                                seed=1)
     ref = oracle.calc_rmse_f64(test, P, Q, b)
-    out = {"shape": f"c3 family at 1%: {spec.m}x{spec.n}, {len(train)} train / {len(test)} test ratings, k=128",
+    del P, Q
+    out = {"shape": f"1% of c3's users: {spec.m}x{spec.n}, {len(train)} train / {len(test)} test ratings, k=128",
            "workers": W, "epochs": 20, "fp64_oracle_rmse": ref, "fp64_oracle_secs": time.time() - t0, "gap": {}}
     prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n)
     tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])

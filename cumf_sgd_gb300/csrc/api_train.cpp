@@ -408,23 +408,16 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
             if (int rc = ckpt_write(ck->path, ckh, d_P.p, d_Q.p, d_dig.as<unsigned long long>(), s)) return rc;
         }
     }
-    if (!sync_each) {
-        float ms = 0;
-        CUMF_CUDA(cudaEventRecord(e1.e, s));
-        CUMF_CUDA(cudaEventSynchronize(e1.e));
-        CUMF_CUDA(cudaEventElapsedTime(&ms, e0.e, e1.e));
-        train_ms = ms;
-    }
+    if (!sync_each) CUMF_CUDA(cudaEventRecord(e1.e, s));
     if (epochs_done) *epochs_done = std::max(first_ep, last_ep);
     const int epochs_run = std::max(0, last_ep - first_ep);
     int status = 0;
     CUMF_CUDA(cudaMemcpyAsync(&status, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    const double t2 = now_ms();
-    trace_epochs.end();
-    TraceRange trace_export("cumf_train: export (fp32, unscale, unpermute, D2H)");
 
     // Export: fp32, unscaled, un-permuted (transform_feature_vector + scale_model + shuffle_model),
-    // into the ratings buffer when it is large enough (it is not read again).
+    // into the ratings buffer when it is large enough (it is not read again).  The export
+    // kernels and copies are queued behind the epochs, and the model's (pinned) host buffers
+    // are allocated while the GPU still runs the epochs.
     const size_t pfb = (size_t)m * k * sizeof(float), qfb = (size_t)n * k * sizeof(float);
     float *pf = nullptr, *qf = nullptr;
     if (d_R.bytes >= pfb + qfb) {
@@ -442,10 +435,19 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     out->b = b;
     cudaError_t ce = cudaMemcpyAsync(out->P, pf, pfb, cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(out->Q, qf, qfb, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess && !sync_each) {
+        ce = cudaEventSynchronize(e1.e);
+        float ms = 0;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0.e, e1.e);
+        train_ms = ms;
+    }
+    const double t2 = now_ms();  // the epochs are done
+    trace_epochs.end();
+    TraceRange trace_export("cumf_train: export (fp32, unscale, unpermute, D2H)");
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
     if (ce != cudaSuccess) {
         cumf_free_model(out);
-        return cuda_fail(ce, "model export");
+        return cuda_fail(ce, "epochs or model export");
     }
     if (status != 0) {
         cumf_free_model(out);

@@ -3,9 +3,10 @@
 An MLP encoder is trained on the tensor cores on (features, solved user row) pairs from plain
 SGD solves of c1-shaped planted matrices; then new users join a deployed c1 model.  Their rows
 initialised by the network must predict their held-out ratings better than every non-learned
-start on the same deployed model (random rows as plain SGD draws them, zero rows, and the
-network's own input: the rating-centred mean of the rated items' factors), far better than
-random rows, and stay better than each after the same fold-in epochs (item rows frozen)."""
+start on the same deployed model (random rows as plain SGD draws them, zero rows, the
+network's own input: the rating-centred mean of the rated items' factors, and the plain mean
+of those factors scaled to the user's mean rating), far better than random rows, and stay
+better than each after the same fold-in epochs (item rows frozen)."""
 import numpy as np
 import pytest
 
@@ -72,8 +73,17 @@ def test_mlp_warm_start_beats_non_learned_new_user_rows(lib, cuda):
     mlp.forward(Xn.data_ptr(), new_users, rows_mlp.data_ptr())
     rng = np.random.default_rng(9)
     rows_rand = torch.from_numpy((rng.random((new_users, K), dtype=np.float32) / np.sqrt(K)).astype(np.float32)).to(cuda)
+    # non-learned: the mean of the rated items' rows scaled so its product with that mean is
+    # the user's mean rating (the model has no bias term)
+    uu = torch.from_numpy(local["u"].astype(np.int64)).to(cuda)
+    vv = torch.from_numpy(local["v"].astype(np.int64)).to(cuda)
+    rr = torch.from_numpy(local["r"].astype(np.float32)).to(cuda)
+    deg = torch.zeros(new_users, device=cuda).index_add_(0, uu, torch.ones_like(rr)).clamp_(min=1)
+    mu = torch.zeros(new_users, device=cuda).index_add_(0, uu, rr) / deg
+    qbar = torch.sparse.mm(torch.sparse_coo_tensor(torch.stack([uu, vv]), 1.0 / deg[uu], (new_users, n)), base_Q)
+    rows_mean = (qbar * (mu / (qbar * qbar).sum(1).clamp_(min=1e-12))[:, None]).contiguous()
     starts = {"mlp": rows_mlp, "random": rows_rand, "zero": torch.zeros(new_users, K, device=cuda),
-              "qmean": Xn[:, :K].contiguous()}
+              "qmean": Xn[:, :K].contiguous(), "mean": rows_mean}
     at_init = {name: new_user_rmse(rows) for name, rows in starts.items()}
     assert at_init["mlp"] < 0.7 * at_init["random"], at_init
     assert all(at_init["mlp"] < v for name, v in at_init.items() if name != "mlp"), at_init
