@@ -174,12 +174,22 @@ __global__ void rmse_kernel(const cumf_node *R, uint64_t nnz, const float *P, ui
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-__global__ void sum_kernel(const double *part, int count, double *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double a = 0.0;
-        for (int i = 0; i < count; ++i) a += part[i];
-        out[0] = a;
+// Sum of `count` partials in a fixed order (one block of kSumThreads): thread t adds
+// part[t], part[t + kSumThreads], ... in index order, then a fixed tree over the threads.
+// The same count always gives the same bits.
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads) sum_kernel(const double *part, int count, double *out) {
+    __shared__ double sh[kSumThreads];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < count; i += kSumThreads) a += part[i];
+    sh[threadIdx.x] = a;
+    __syncthreads();
+#pragma unroll
+    for (int w = kSumThreads / 2; w >= 1; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
     }
+    if (threadIdx.x == 0) out[0] = sh[0];
 }
 
 int grid_for(uint64_t items, int per_thread = 1) {
@@ -282,7 +292,7 @@ cudaError_t launch_rmse(const cumf_node *d_R, int64_t nnz, const float *P, int32
                         double *d_sum, cudaStream_t s) {
     rmse_kernel<<<kReduceBlocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, P, (uint32_t)m, Q,
                                                    (uint32_t)n, k, b, d_part);
-    sum_kernel<<<1, 32, 0, s>>>(d_part, kReduceBlocks, d_sum);
+    sum_kernel<<<1, kSumThreads, 0, s>>>(d_part, kReduceBlocks, d_sum);
     return cudaGetLastError();
 }
 
@@ -313,7 +323,7 @@ cudaError_t launch_rmse_grid(const cumf_node *d_R, int64_t nnz, const float *P, 
                              const float *Q, int32_t n, int k, float b, int blocks,
                              double *d_part, double *d_sum, cudaStream_t s) {
     rmse_kernel<<<blocks, kThreads, 0, s>>>(d_R, (uint64_t)nnz, P, (uint32_t)m, Q, (uint32_t)n, k, b, d_part);
-    sum_kernel<<<1, 32, 0, s>>>(d_part, blocks, d_sum);
+    sum_kernel<<<1, kSumThreads, 0, s>>>(d_part, blocks, d_sum);
     return cudaGetLastError();
 }
 
