@@ -305,6 +305,11 @@ def sgd_train(tr: MFProblem, va: Optional[MFProblem], param: Parameter,
     return model
 
 
+def release_host_cache() -> None:
+    """Gives the cached page-locked host buffers back to the system (cumf_release_host_cache)."""
+    _lib.check(_lib.load().cumf_release_host_cache())
+
+
 def save_model(model: MFModel, path: str) -> None:
     """save_model (singleGPU/main.cpp:231-273)."""
     _lib.check(_lib.load().cumf_save_model(C.byref(model._c), path.encode()))

@@ -155,6 +155,7 @@ _SIGS = {
                                  C.POINTER(C.c_double), _VP]),
     "cumf_train_ex": (C.c_int, [C.POINTER(Problem), C.POINTER(Problem), C.POINTER(Params), C.POINTER(Model),
                                 C.POINTER(Model), C.POINTER(TrainStats), _VP, _VP]),
+    "cumf_release_host_cache": (C.c_int, []),
     "cumf_batch_create": (C.c_int, [C.POINTER(BatchProblem), C.c_int, C.POINTER(C.c_void_p)]),
     "cumf_batch_destroy": (C.c_int, [_VP]),
     "cumf_batch_set_tuning": (C.c_int, [_VP, C.POINTER(BatchTuning)]),

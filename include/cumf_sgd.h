@@ -195,6 +195,12 @@ int cumf_save_model(const cumf_model *model, const char *path);
 int cumf_load_model(const char *path, cumf_model *out);
 int cumf_alloc_model(int32_t m, int32_t n, int32_t k, cumf_model *out);
 int cumf_free_model(cumf_model *model);
+/* Page-locked host buffers (pinned problems, models) are cached: cumf_free_problem and
+ * cumf_free_model keep them (up to 2 GB in all) for the next pinned allocation they fit,
+ * because page-locking costs about 30 ms per GB and training calls repeat.  No counterpart
+ * in the reference (which leaks its pinned buffers).  This call gives the cached buffers
+ * back to the system; buffers still held by problems or models are not affected. */
+int cumf_release_host_cache(void);
 
 /* ---- rating text (data/netflix/transform.cpp) --------------------------------------- */
 

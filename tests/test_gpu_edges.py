@@ -1,5 +1,5 @@
 """Edge cases of the update path: factor rows beyond 4 GB of offset, a rating array longer
-than 2^31 records, and empty problems in every mode."""
+than 2^31 records, and empty problems in every mode; the cache of page-locked host buffers."""
 import numpy as np
 import pytest
 
@@ -115,3 +115,34 @@ def test_copy_bandwidth_probe(lib, cuda):
     assert hbm.value > 1000 and l2.value > 1.3 * hbm.value
     with pytest.raises(cm.CumfError):
         _lib.check(lib.cumf_probe_copy_bandwidth(8, 1, C.byref(l2), None))
+
+
+def test_pinned_host_buffers_are_cached_and_released(lib, cuda):
+    """A pinned model buffer given back by cumf_free_model serves the next allocation it fits
+    (page-locking is the slow part of every training call's export); a request much smaller
+    than the cached block gets its own; cumf_release_host_cache empties the cache."""
+    import ctypes as C
+    from cumf_sgd_gb300 import _lib
+    lib.cumf_release_host_cache()
+
+    def alloc(m, n, k):
+        mod = _lib.Model()
+        assert lib.cumf_alloc_model(m, n, k, C.byref(mod)) == 0
+        assert mod.pinned == 1
+        return mod
+
+    a = alloc(20_000, 3_000, 128)
+    p_addr, q_addr = C.cast(a.P, C.c_void_p).value, C.cast(a.Q, C.c_void_p).value
+    assert lib.cumf_free_model(C.byref(a)) == 0
+    b = alloc(20_000, 3_000, 128)  # the same sizes come back from the cache
+    assert C.cast(b.P, C.c_void_p).value == p_addr and C.cast(b.Q, C.c_void_p).value == q_addr
+    arr = np.ctypeslib.as_array(b.P, shape=(20_000 * 128,))
+    arr[:] = 1.5  # the reused buffer is ordinary writable host memory
+    assert lib.cumf_free_model(C.byref(b)) == 0
+    tiny = alloc(10, 10, 128)  # far smaller than the cached P block: not taken from it
+    assert C.cast(tiny.P, C.c_void_p).value != p_addr
+    assert lib.cumf_free_model(C.byref(tiny)) == 0
+    assert lib.cumf_release_host_cache() == 0
+    c = alloc(20_000, 3_000, 128)
+    assert lib.cumf_free_model(C.byref(c)) == 0
+    assert lib.cumf_release_host_cache() == 0
