@@ -5,7 +5,8 @@ oracle/ref_build.sh; its update kernel is sgd_k128_kernel_hogwild_warp32_lrate
 (sgd_k128_kernel_hogwild_warp32.h:3-104).  Both trainers get the same 12-byte training file
 and the reference's canonical flags (data/netflix/run.sh:3: -l 0.05 -a 0.08 -b 0.3 -k 128
 -t 20 -u 1 -v 1 -x 1 -y 1) with -s 52 x SMs (README.md:61, 7,904 workers on 152 SMs); both
-models are scored by the same evaluator (calc_rmse, pinned to test/mf.cpp:3815-3839).
+models are scored by the same evaluator (calc_rmse, pinned to test/mf.cpp:3815-3839), and
+every score is checked against the reference's own mf-predict -e 0 (4 printed decimals).
 
 Bound: 0.002 test RMSE.
   - 480,189 x 17,770, 99M ratings (the benchmark shape): |ours - reference| <= 0.002.
@@ -56,18 +57,26 @@ def _compare(ref_tools, spec, tmp_path, reps):
     sm, _, _ = cm.device_info(0)
     workers = 52 * sm
     train, test = synth.generate(spec, seed=0, device="cuda")
-    tr_path = str(tmp_path / "train.bin")
+    tr_path, te_path = str(tmp_path / "train.bin"), str(tmp_path / "test.bin")
     ref_tools.write_records(train, tr_path)
+    ref_tools.write_records(test, te_path)
     te = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+
+    def score(model_path):
+        got = cm.calc_rmse(te, cm.load_model(model_path))
+        if ref_tools.available("mf-predict"):  # the reference's evaluator prints 4 decimals
+            assert abs(ref_tools.libmf_rmse(te_path, model_path) - got) <= 6e-5, model_path
+        return got
+
     ref, ours = [], []
     for rep in range(reps):
         mp = str(tmp_path / "ref.model")
         out = ref_tools.run_reference_gpu(tr_path, mp, workers, 20)
         assert out["rc"] == 0 and out["update_per_sec"], out
-        ref.append(cm.calc_rmse(te, cm.load_model(mp)))
+        ref.append(score(mp))
         mo = str(tmp_path / "ours.model")
         _ours(tr_path, mo, workers, rep + 1)
-        ours.append(cm.calc_rmse(te, cm.load_model(mo)))
+        ours.append(score(mo))
     return float(np.mean(ref)), float(np.mean(ours)), ref, ours
 
 
