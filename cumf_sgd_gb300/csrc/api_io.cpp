@@ -46,9 +46,18 @@ int cuda_fail(cudaError_t e, const char *what) {
 // cumf_free_problem is kept, and the next pinned request it fits (between half its size and
 // its size) takes it again.  Page-locking costs about 30 ms per GB on the GB300 host (8 ms
 // for a 480,189 x 17,770 x 128 model), which repeated training calls then pay once.  At most
-// kPinnedCacheBytes stay cached; cumf_release_host_cache gives them back to the system.
+// 2 GB stay cached (the environment variable CUMF_HOST_CACHE_MB sets another limit, 0 turns
+// the cache off); cumf_release_host_cache gives them back to the system.
 namespace {
-constexpr size_t kPinnedCacheBytes = size_t(2) << 30;
+size_t pinned_cache_limit() {
+    static const size_t limit = [] {
+        const char *e = getenv("CUMF_HOST_CACHE_MB");
+        if (!e || !*e) return size_t(2) << 30;
+        const long long mb = atoll(e);
+        return mb > 0 ? (size_t)mb << 20 : size_t(0);
+    }();
+    return limit;
+}
 struct PinnedCache {
     std::mutex mu;
     std::vector<std::pair<void *, size_t>> free_blocks;  // cached, not in use
@@ -108,7 +117,7 @@ static void host_free(void *p, int pinned) {
         if (c.live[i].first != p) continue;
         const auto blk = c.live[i];
         c.live.erase(c.live.begin() + i);
-        if (c.cached_bytes + blk.second <= kPinnedCacheBytes) {
+        if (c.cached_bytes + blk.second <= pinned_cache_limit()) {
             c.free_blocks.push_back(blk);
             c.cached_bytes += blk.second;
             return;

@@ -196,7 +196,8 @@ int cumf_load_model(const char *path, cumf_model *out);
 int cumf_alloc_model(int32_t m, int32_t n, int32_t k, cumf_model *out);
 int cumf_free_model(cumf_model *model);
 /* Page-locked host buffers (pinned problems, models) are cached: cumf_free_problem and
- * cumf_free_model keep them (up to 2 GB in all) for the next pinned allocation they fit,
+ * cumf_free_model keep them (up to 2 GB in all, or CUMF_HOST_CACHE_MB megabytes from the
+ * environment; 0 turns the cache off) for the next pinned allocation they fit,
  * because page-locking costs about 30 ms per GB and training calls repeat.  No counterpart
  * in the reference (which leaks its pinned buffers).  This call gives the cached buffers
  * back to the system; buffers still held by problems or models are not affected. */
