@@ -1075,7 +1075,7 @@ def main():
                "h2d_bytes_per_step": nnz * 12 + 4 * (m + n), "d2h_bytes_per_step": 4 * K * (m + n),
                "epochs_per_step": args.e2e_epochs, "wall_s": wall,
                "prep_ms": st.prep_ms, "train_ms": st.train_ms, "export_ms": st.export_ms,
-               "test_rmse": test_rmse}
+               "model_pinned": int(model._c.pinned), "test_rmse": test_rmse}
         del model
 
     # The benchmark shape at the reference's recommended worker count (52 per SM,
