@@ -940,6 +940,8 @@ def main():
     ap.add_argument("--l2-hints", type=int, default=-1, help="L2 eviction hints 0/1 (-1: default)")
     ap.add_argument("--ring", type=int, default=-1, help="shared-memory row ring 0/1 (-1: default)")
     ap.add_argument("--e2e-epochs", type=int, default=20)
+    ap.add_argument("--hot-rows", type=float, default=None,
+                    help="expected workers per copy of a most-rated row (default: the library's; 0 = no copies)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the time-to-target measurement")
@@ -1012,10 +1014,20 @@ def main():
     cm.dev_shuffle_scale(d_raw.data_ptr(), d_R.data_ptr(), nnz, pm.data_ptr(), m, qm.data_ptr(), n,
                          float(np.float32(1.0 / float(scale))), 0, sp)
     del d_raw
-    P = torch.empty(m * K * eb, dtype=torch.uint8, device=dev)
-    Q = torch.empty(n * K * eb, dtype=torch.uint8, device=dev)
+    # Copies of the most-rated rows, laid out and assigned as cumf_train does by default.
+    conc = args.hot_rows if args.hot_rows is not None else float(cm.Parameter().to_c().hot_rows)
+    per_copy = cm.HotRows.per_copy(nnz, workers, K, prec, args.lanes, conc)
+    hot = cm.HotRows(d_R.data_ptr(), nnz, m, n, per_copy, stream=sp) if per_copy > 0 else None
+    m_rows, n_rows = (hot.m_rows, hot.n_rows) if hot else (m, n)
+    if hot:
+        hot.assign(d_R.data_ptr(), nnz, sp)
+    P = torch.empty(m_rows * K * eb, dtype=torch.uint8, device=dev)
+    Q = torch.empty(n_rows * K * eb, dtype=torch.uint8, device=dev)
     cm.dev_init_factors(P.data_ptr(), m, K, prec, rank, 1, sp)
     cm.dev_init_factors(Q.data_ptr(), n, K, prec, rank, 2, sp)
+    merges = hot is not None and hot.hot_users + hot.hot_items > 0
+    if merges:
+        hot.spread(P.data_ptr(), Q.data_ptr(), K, prec, sp)
     # Step s runs epoch s mod 20 of the 20-epoch job's learning-rate schedule.
     job_epochs = 20
     epochs_total = args.warmup + args.steps
@@ -1024,9 +1036,11 @@ def main():
     status = torch.zeros(1, dtype=torch.int32, device=dev)
 
     def epoch(e):
-        cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m, Q.data_ptr(), n, K, prec, workers, args.lanes,
+        cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m_rows, Q.data_ptr(), n_rows, K, prec, workers, args.lanes,
                       lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp,
                       prefetch=args.prefetch, l2_hints=args.l2_hints, ring=args.ring)
+        if merges:
+            hot.merge(P.data_ptr(), Q.data_ptr(), K, prec, sp)
 
     for e in range(args.warmup):
         epoch(e)
@@ -1054,8 +1068,10 @@ def main():
     peak, peak_kind = measured_peaks()
     l2_gbs = l2_copy_gbs()
 
-    # Test RMSE of the device-resident run (for the record).
-    del P, Q, d_R
+    hot_info = {"concurrency": conc, "per_copy": per_copy, "hot_users": hot.hot_users if hot else 0,
+                "hot_items": hot.hot_items if hot else 0,
+                "extra_rows": (m_rows - m) + (n_rows - n)}
+    del P, Q, d_R, hot
     torch.cuda.empty_cache()
 
     # End to end through the C ABI: pinned host ratings -> cumf_train (20 epochs) -> fp32 model.
@@ -1064,7 +1080,8 @@ def main():
         prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=m, n=n, pinned=True)
         tprob = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
         par = cm.Parameter(k=K, num_workers=workers, num_iters=args.e2e_epochs, lambda_p=0.05, lambda_q=0.05,
-                           alpha=0.08, beta=0.3, seed=rank, gpu=local, precision=prec, lanes=args.lanes)
+                           alpha=0.08, beta=0.3, seed=rank, gpu=local, precision=prec, lanes=args.lanes,
+                           hot_rows=args.hot_rows)
         cm.sgd_train(prob, None, cm.Parameter(**{**par.__dict__, "num_iters": 1}))  # warm-up call
         barrier(world)
         t0 = time.perf_counter()
@@ -1075,7 +1092,8 @@ def main():
                "h2d_bytes_per_step": nnz * 12 + 4 * (m + n), "d2h_bytes_per_step": 4 * K * (m + n),
                "epochs_per_step": args.e2e_epochs, "wall_s": wall,
                "prep_ms": st.prep_ms, "train_ms": st.train_ms, "export_ms": st.export_ms,
-               "model_pinned": int(model._c.pinned), "test_rmse": test_rmse}
+               "model_pinned": int(model._c.pinned), "test_rmse": test_rmse,
+               "hot_rows": {"hot_users": st.hot_users, "hot_items": st.hot_items, "extra_rows": st.extra_rows}}
         del model
 
     # The benchmark shape at the reference's recommended worker count (52 per SM,
@@ -1186,7 +1204,10 @@ def main():
                 "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": prec, "data": "synthetic",
                 "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz, "k": K, "storage": prec,
-                           "workers": workers, "lanes": args.lanes or "auto", "step": "one epoch (one launch)",
+                           "workers": workers, "lanes": args.lanes or "auto",
+                           "step": ("one epoch (update launch + merge of the row copies)" if merges
+                                    else "one epoch (one launch)"),
+                           "hot_rows": hot_info,
                            "samples_per_epoch": samples_per_launch,
                            "l2": "inputs larger than L2 (ratings 1.19 GB)", "parallelism": f"replicas{world}"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -1196,7 +1217,7 @@ def main():
                              "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
                 "l2_roofline": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
                                 "peak_kind": "L2-resident copy (2 x 16 MB, 400 passes in one launch), measured in this run"},
-                "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps, "cpu_baseline": cpu,
+                "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps * (2 if merges else 1), "cpu_baseline": cpu,
                 "cpu_port": cpu_port, "fp64_oracle": fp64, "value_w52": w52, "reference_kernel": refk,
                 "time_to_target": ttt, "time_to_target_c1": ttt_c1, "batched": batched,
                 "precision_gap": precision_gap}

@@ -55,6 +55,7 @@ class Parameter:
     tail_epochs: int = 0
     tail_start: int = 0
     deterministic: int = 0
+    hot_rows: Optional[float] = None  # expected workers per copy of a most-rated row; None = library default
 
     @property
     def ux(self) -> int:
@@ -76,6 +77,8 @@ class Parameter:
         p.quiet = int(bool(self.quiet))
         p.verbose_epochs = int(bool(self.verbose_epochs))
         p.ux, p.vy = self.ux, self.vy
+        if self.hot_rows is not None:
+            p.hot_rows = float(self.hot_rows)
         return p
 
     @staticmethod
@@ -85,7 +88,7 @@ class Parameter:
                          x_grid=p.x_grid, y_grid=p.y_grid, num_iters=p.num_iters, gpu=p.gpu,
                          lambda_p=p.lambda_p, lambda_q=p.lambda_q, lrate=p.lrate, alpha=p.alpha,
                          beta=p.beta, seed=p.seed, precision=inv[p.precision], lanes=p.lanes,
-                         quiet=bool(p.quiet))
+                         quiet=bool(p.quiet), deterministic=p.deterministic, hot_rows=p.hot_rows)
 
 
 @dataclasses.dataclass
@@ -287,6 +290,9 @@ class TrainStats:
     mode: int
     num_workers: int
     lanes: int
+    hot_users: int = 0
+    hot_items: int = 0
+    extra_rows: int = 0
 
 
 def sgd_train(tr: MFProblem, va: Optional[MFProblem], param: Parameter,
@@ -432,6 +438,58 @@ def dev_rating_stats(d_R: int, nnz: int, stream: int = 0):
     _lib.check(_lib.load().cumf_dev_rating_stats(d_R, nnz, C.byref(mean), C.byref(std),
                                                  stream or None))
     return mean.value, std.value
+
+
+class HotRows:
+    """Copies of the most-rated rows (cumf_hot_rows_*): plan, assign, spread, merge."""
+
+    def __init__(self, d_R: int, nnz: int, m: int, n: int, per_copy: int, max_copies: int = 256,
+                 stream: int = 0):
+        self._lib = _lib.load()
+        self._h = C.c_void_p()
+        _lib.check(self._lib.cumf_hot_rows_plan(d_R, nnz, m, n, per_copy, max_copies, C.byref(self._h),
+                                                stream or None))
+        mr, nr, hm, hn = (C.c_int32() for _ in range(4))
+        _lib.check(self._lib.cumf_hot_rows_info(self._h, C.byref(mr), C.byref(nr), C.byref(hm), C.byref(hn)))
+        self.m, self.n = m, n
+        self.m_rows, self.n_rows, self.hot_users, self.hot_items = mr.value, nr.value, hm.value, hn.value
+
+    @staticmethod
+    def per_copy(nnz: int, num_workers: int, k: int, precision: str, lanes: int, concurrency: float) -> int:
+        return int(_lib.load().cumf_hot_rows_per_copy(nnz, num_workers, k, PRECISIONS[precision], lanes,
+                                                      concurrency))
+
+    def tables(self):
+        """Host copies: (tab_m (m x 2), tab_n (n x 2), grp_m, grp_n); tab rows are {copies, first extra row}."""
+        tm = np.zeros((self.m, 2), np.int32)
+        tn = np.zeros((self.n, 2), np.int32)
+        gm = np.zeros(max(1, self.hot_users), np.int32)
+        gn = np.zeros(max(1, self.hot_items), np.int32)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        _lib.check(self._lib.cumf_hot_rows_tables(self._h, p(tm), p(tn), p(gm), p(gn)))
+        return tm, tn, gm[:self.hot_users], gn[:self.hot_items]
+
+    def assign(self, d_R: int, nnz: int, stream: int = 0) -> None:
+        _lib.check(self._lib.cumf_hot_rows_assign(self._h, d_R, nnz, stream or None))
+
+    def spread(self, d_P: int, d_Q: int, k: int, precision: str, stream: int = 0) -> None:
+        _lib.check(self._lib.cumf_hot_rows_spread(self._h, d_P or None, d_Q or None, k, PRECISIONS[precision],
+                                                  stream or None))
+
+    def merge(self, d_P: int, d_Q: int, k: int, precision: str, stream: int = 0) -> None:
+        _lib.check(self._lib.cumf_hot_rows_merge(self._h, d_P or None, d_Q or None, k, PRECISIONS[precision],
+                                                 stream or None))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.cumf_hot_rows_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def dev_rmse(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, b: float,

@@ -46,7 +46,7 @@ class Params(C.Structure):
                 ("quiet", C.c_int32), ("epochs_per_launch", C.c_int32),
                 ("verbose_epochs", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
                 ("ring", C.c_int32), ("tail_epochs", C.c_int32), ("deterministic", C.c_int32),
-                ("tail_start", C.c_int64)]
+                ("tail_start", C.c_int64), ("hot_rows", C.c_float), ("reserved_", C.c_int32 * 3)]
 
 
 class Tuning(C.Structure):
@@ -70,7 +70,8 @@ class TrainStats(C.Structure):
                 ("total_ms", C.c_double), ("updates_per_sec", C.c_double),
                 ("samples_per_epoch", C.c_int64), ("mean", C.c_float), ("std_dev", C.c_float),
                 ("mode", C.c_int32), ("num_workers", C.c_int32), ("lanes", C.c_int32),
-                ("reserved_", C.c_int32 * 5)]
+                ("hot_users", C.c_int32), ("hot_items", C.c_int32), ("extra_rows", C.c_int32),
+                ("reserved_", C.c_int32 * 2)]
 
 
 class BatchProblem(C.Structure):
@@ -94,6 +95,16 @@ class Args(C.Structure):
 _VP = C.c_void_p
 _SIGS = {
     "cumf_abi_version": (C.c_int, []),
+    "cumf_hot_rows_per_copy": (C.c_int64, [C.c_int64, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_float]),
+    "cumf_hot_rows_plan": (C.c_int, [_VP, C.c_int64, C.c_int32, C.c_int32, C.c_int64, C.c_int32,
+                                     C.POINTER(_VP), _VP]),
+    "cumf_hot_rows_info": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    "cumf_hot_rows_tables": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "cumf_hot_rows_assign": (C.c_int, [_VP, _VP, C.c_int64, _VP]),
+    "cumf_hot_rows_spread": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, _VP]),
+    "cumf_hot_rows_merge": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, _VP]),
+    "cumf_hot_rows_free": (C.c_int, [_VP]),
     "cumf_last_error": (C.c_char_p, []),
     "cumf_default_params": (C.c_int, [C.POINTER(Params)]),
     "cumf_parse_args": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Args)]),

@@ -38,6 +38,7 @@ LIB_SOURCES = [
     "text_parse.cu",
     "eval.cu",
     "strata.cu",
+    "hot_rows.cu",
 ]
 TOOLS = {"cumf_sgd": "cli_main.cpp", "cumf_predict": "predict_main.cpp", "cumf_transform": "transform_main.cpp"}
 

@@ -200,6 +200,7 @@ int cumf_default_params(cumf_params *p) {
     p->prefetch = -1;
     p->l2_hints = -1;
     p->ring = -1;
+    p->hot_rows = kHotDefaultConcurrency;
     return CUMF_OK;
 }
 
@@ -328,6 +329,12 @@ int cumf_parse_args(int argc, char **argv, cumf_args *out) {
             ++i;
             if (!is_numerical(argv[i])) return fail(CUMF_ERR_ARG, "--deterministic should be followed by a number");
             p.deterministic = atoi(argv[i]);
+        } else if (a == "--hot-rows") {
+            if (!need(i, "need to specify a number after --hot-rows")) return CUMF_ERR_ARG;
+            ++i;
+            if (!is_numerical(argv[i])) return fail(CUMF_ERR_ARG, "--hot-rows should be followed by a number");
+            p.hot_rows = (float)atof(argv[i]);
+            if (!(p.hot_rows >= 0.f)) return fail(CUMF_ERR_ARG, "--hot-rows should be 0 or more");
         } else {
             break;
         }

@@ -85,11 +85,22 @@ struct CkptHeader {
     char magic[8];
     int32_t version, k, precision, workers, lanes, num_iters, epochs_done, m, n, tail_epochs, reserved;
     uint64_t seed;
-    float lambda_p, lambda_q, alpha, beta, lrate, pad;
+    float lambda_p, lambda_q, alpha, beta, lrate, hot_rows;
     int64_t nnz, tail_start;
     uint64_t records_digest, bytes_p, bytes_q, payload_digest;
 };
 constexpr char kCkptMagic[8] = {'C', 'U', 'M', 'F', 'C', 'K', 'P', '1'};
+
+// The copies of the most-rated rows of one training call.
+struct HotRows {
+    cumf_hot_rows *h = nullptr;
+    HotRows() = default;
+    HotRows(const HotRows &) = delete;
+    HotRows &operator=(const HotRows &) = delete;
+    ~HotRows() {
+        if (h) cumf_hot_rows_free(h);
+    }
+};
 
 struct PinnedHost {
     void *p = nullptr;
@@ -157,6 +168,7 @@ int ckpt_read(const char *path, const CkptHeader &want, void *d_P, void *d_Q, un
         return bad("training ratings");
     if (h.tail_epochs != want.tail_epochs || h.tail_start != want.tail_start) return bad("fold-in epochs");
     if (h.reserved != want.reserved) return bad("schedule (batch-Hogwild or deterministic grid)");
+    if (h.hot_rows != want.hot_rows) return bad("copies of the most-rated rows (hot_rows)");
     if (h.bytes_p != want.bytes_p || h.bytes_q != want.bytes_q) return bad("factor sizes");
     if (h.epochs_done < 0 || h.epochs_done > want.num_iters) return bad("more epochs done than this run has");
     PinnedHost buf;
@@ -228,10 +240,34 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
                                    d_qmap.as<int32_t>(), n, rscale, d_status.as<int>(), s));
     const float lambda_p = p.lambda_p / pr.scale, lambda_q = p.lambda_q / pr.scale;  // sgd.cu:673-674
 
+    // Copies of the most-rated rows (batch-Hogwild only): laid out from the ratings' counts,
+    // and every rating of such a row rewritten to name its copy.
+    const int strata_g = p.deterministic > 0 ? strata_groups(nnz, p.deterministic) : 0;
+    HotRows hot;
+    int32_t m_rows = m, n_rows = n;
+    if (strata_g == 0 && p.tail_epochs <= 0 && nnz > 0) {
+        int dev_h = 0, sms_h = 0;
+        CUMF_CUDA(cudaGetDevice(&dev_h));
+        CUMF_CUDA(cudaDeviceGetAttribute(&sms_h, cudaDevAttrMultiProcessorCount, dev_h));
+        const int64_t per_copy = hot_rows_per_copy(nnz, workers, k, p.precision, lanes, p.hot_rows, sms_h);
+        if (per_copy > 0) {
+            if (int rc = cumf_hot_rows_plan(d_R.as<cumf_node>(), nnz, m, n, per_copy, kHotMaxCopies, &hot.h, s))
+                return rc;
+            int32_t hm = 0, hn = 0;
+            cumf_hot_rows_info(hot.h, &m_rows, &n_rows, &hm, &hn);
+            if (hm + hn == 0) {
+                cumf_hot_rows_free(hot.h);
+                hot.h = nullptr;
+            } else if (int rc = cumf_hot_rows_assign(hot.h, d_R.as<cumf_node>(), nnz, s)) {
+                return rc;
+            }
+        }
+    }
+
     // init_model: every row, including rows without ratings (sgd.cu:548-591).
     const int eb = elem_bytes(p.precision);
-    CUMF_CUDA(d_P.alloc((size_t)m * k * eb));
-    CUMF_CUDA(d_Q.alloc((size_t)n * k * eb));
+    CUMF_CUDA(d_P.alloc((size_t)m_rows * k * eb));
+    CUMF_CUDA(d_Q.alloc((size_t)n_rows * k * eb));
     CUMF_CUDA(launch_init_factors(d_P.p, m, k, p.precision, p.seed, 1, s));
     CUMF_CUDA(launch_init_factors(d_Q.p, n, k, p.precision, p.seed, 2, s));
     if (init) {  // starting factors for the first init->m users and init->n items
@@ -259,6 +295,8 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         }
         CUMF_CUDA(cudaStreamSynchronize(s));
     }
+    if (hot.h)
+        if (int rc = cumf_hot_rows_spread(hot.h, d_P.p, d_Q.p, k, p.precision, s)) return rc;
 
     std::vector<float> lr(std::max(1, p.num_iters + 4));
     cumf_lr_schedule(p.alpha, p.beta, p.lrate, (int)lr.size(), lr.data());
@@ -266,7 +304,6 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
     CUMF_CUDA(cudaMemcpyAsync(d_lr.p, lr.data(), lr.size() * sizeof(float), cudaMemcpyHostToDevice, s));
 
     // Deterministic schedule: the shuffled, scaled ratings stably sorted into G x G blocks.
-    const int strata_g = p.deterministic > 0 ? strata_groups(nnz, p.deterministic) : 0;
     DevBuf d_S, d_off;
     if (strata_g > 0 && nnz > 0) {
         CUMF_CUDA(d_S.alloc((size_t)nnz * sizeof(cumf_node)));
@@ -336,8 +373,9 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         ckh.nnz = nnz;
         ckh.tail_start = p.tail_start;
         ckh.records_digest = records_digest;
-        ckh.bytes_p = (uint64_t)m * k * eb;
-        ckh.bytes_q = (uint64_t)n * k * eb;
+        ckh.hot_rows = hot.h ? p.hot_rows : 0.f;
+        ckh.bytes_p = (uint64_t)m_rows * k * eb;
+        ckh.bytes_q = (uint64_t)n_rows * k * eb;
         if (ck->resume) {
             bool found = false;
             int32_t done = 0;
@@ -379,9 +417,11 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
                                            d_status.as<int>(), s))
                     return rc;
         } else {
-            CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m, d_Q.p, n, k, p.precision, workers_ep, tu,
+            CUMF_CUDA(launch_sgd_update(R_ep, nnz_ep, d_P.p, m_rows, d_Q.p, n_rows, k, p.precision, workers_ep, tu,
                                         d_lr.as<float>(), ep, cnt, lambda_p, lambda_q, p.seed, d_status.as<int>(), s,
                                         &lanes_used));
+            if (hot.h)
+                if (int rc = cumf_hot_rows_merge(hot.h, d_P.p, d_Q.p, k, p.precision, s)) return rc;
         }
         float ms = 0;
         if (sync_each) {
@@ -466,6 +506,8 @@ int train_mode_a(const cumf_problem *tr, const cumf_problem *va, const cumf_para
         st->mode = 0;
         st->num_workers = strata_g > 0 ? strata_g : workers;  // deterministic: workers per stratum
         st->lanes = lanes_used;
+        if (hot.h) cumf_hot_rows_info(hot.h, nullptr, nullptr, &st->hot_users, &st->hot_items);
+        st->extra_rows = (m_rows - m) + (n_rows - n);
     }
     if (!p.quiet) {
         printf("update_per_sec:%f\n", train_ms > 0 ? (double)nnz * epochs_run / (train_ms * 1e-3) : 0.0);

@@ -4,7 +4,7 @@
 //            [-s workers] [-u U] [-v V] [-x X] [-y Y] [-p test_file]
 //            [--seed N] [--precision fp16|bf16|fp32|bf16sr|fp16sr] [--lanes N] [--quiet]
 //            [--checkpoint path [--checkpoint-every N] [--resume]] [--deterministic G]
-//            train_file [model_file]
+//            [--hot-rows X] train_file [model_file]
 //
 // Exit status 1 on bad arguments (main.cpp:286-289); unlike the reference, a failed read,
 // training or model write also exits non-zero with the library's message.  With -p the
@@ -12,6 +12,8 @@
 // --checkpoint writes the in-HBM factors every N epochs (default 1; mode A only) and
 // --resume continues from a matching checkpoint (cumf_train_ckpt).  --deterministic 1 (or a
 // grid size G) trains with the bit-reproducible stratified schedule instead of batch-Hogwild.
+// --hot-rows X sets the expected workers per copy of a most-rated row (0: no copies, every
+// rating updates its own row as in the reference).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>

@@ -133,6 +133,16 @@ int strata_epochs(const cumf_node *d_S, const unsigned long long *d_block_off, i
                   void *d_Q, int32_t n, int k, int precision, const float *h_lr, int first_epoch, int n_epochs,
                   float lambda_p, float lambda_q, uint64_t seed, int *d_status, cudaStream_t s);
 
+// ---- hot_rows.cu (copies of the most-rated rows) ----------------------------------------
+// A copy carries at least this many ratings an epoch, and a row has at most kHotMaxCopies.
+constexpr int64_t kHotMinPerCopy = 4096;
+constexpr int kHotMaxCopies = 256;
+// cumf_params.hot_rows of cumf_default_params: expected workers per copy.
+constexpr float kHotDefaultConcurrency = 0.5f;
+// Ratings per copy for `concurrency` expected workers on one copy at a time (0 = no copies:
+// concurrency <= 0, fewer than two workers or no ratings).
+int64_t hot_rows_per_copy(int64_t nnz, int32_t num_workers, int k, int precision, int lanes, float concurrency,
+                          int sm_count);
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }
 

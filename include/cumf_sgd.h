@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define CUMF_ABI_VERSION 1
+#define CUMF_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------------- */
 enum {
@@ -110,6 +110,10 @@ typedef struct cumf_params {
                               automatic grid; > 1 = that many user / item groups            */
     int64_t tail_start;    /* (tail_epochs) [tail_start, nnz) (e.g. newly added users'
                               ratings): those epochs update user rows only (item rows frozen) */
+    float hot_rows;        /* batch-Hogwild, mode A: copies of the most-rated rows
+                              (cumf_hot_rows_*) for this many expected workers per copy;
+                              0 = none (every rating updates its own row, as the reference) */
+    int32_t reserved_[3];
 } cumf_params;
 
 /* Launch tuning of the update kernel (the knobs the autotuner searches). */
@@ -152,7 +156,9 @@ typedef struct cumf_train_stats {
     int32_t mode;          /* 0 = A (in HBM), 1 = B (u x v), 2 = C (x x y streaming)    */
     int32_t num_workers;
     int32_t lanes;
-    int32_t reserved_[5];
+    int32_t hot_users, hot_items;  /* rows given copies (cumf_params.hot_rows)           */
+    int32_t extra_rows;            /* rows added to P and Q for those copies               */
+    int32_t reserved_[2];
 } cumf_train_stats;
 
 /* CLI arguments: Argument (singleGPU/sgd.h:48-77). */
@@ -167,11 +173,12 @@ typedef struct cumf_args {
 int cumf_abi_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 const char *cumf_last_error(void);
-/* Reference defaults (singleGPU/sgd.h:45) plus seed 0, FP16, auto lanes. */
+/* Reference defaults (singleGPU/sgd.h:45) plus seed 0, FP16, auto lanes, hot_rows 0.5. */
 int cumf_default_params(cumf_params *p);
 /* parse_argument (singleGPU/main.cpp:33-227): same flags, same -s rounding, the same
  * default model path (<basename of train file>.model), u*v==1 forces x=y=1.  Long flags
- * added: --seed N, --precision fp16|bf16|fp32|bf16sr|fp16sr, --lanes N, --quiet.
+ * added: --seed N, --precision fp16|bf16|fp32|bf16sr|fp16sr, --lanes N, --quiet,
+ * --deterministic G, --hot-rows X (cumf_params.hot_rows; 0 = off).
  * Returns CUMF_ERR_ARG with the reference's message on bad input. */
 int cumf_parse_args(int argc, char **argv, cumf_args *out);
 
@@ -292,6 +299,51 @@ int cumf_sgd_update_tuned(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t 
                           const cumf_tuning *tuning, const float *d_lr, int first_epoch,
                           int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
                           int *d_status, void *stream);
+
+/* ---- copies of the most-rated rows (no counterpart in the reference) -----------------
+ * Batch-Hogwild workers that hold the same user or item row at the same moment serialise on
+ * its cache lines; with skewed ids (Zipf item popularity) that bounds the epoch.  A row with
+ * more than `per_copy` ratings gets min(max_copies, ceil(count / per_copy)) copies: the row
+ * itself plus extra rows appended after the matrix's last row (rows m .. m_rows-1 of P,
+ * n .. n_rows-1 of Q, in row order).  Rating i of such a row is assigned copy i mod copies.
+ * The copies start equal (spread) and are averaged after each launch of epochs (merge: the
+ * fp32 mean in copy order, rounded to nearest in the storage type, written to every copy),
+ * so between launches every copy holds the row's value and exports read the row itself.
+ * Use: plan on the shuffled, scaled ratings; allocate P and Q with m_rows and n_rows rows;
+ * assign (rewrites the ratings' ids in place); init the first m / n rows; spread; then
+ * cumf_sgd_update(..., m_rows, ..., n_rows, ...) and merge after every call.
+ * cumf_train does this when params.hot_rows > 0. */
+typedef struct cumf_hot_rows cumf_hot_rows;
+
+/* Ratings per copy for `concurrency` expected workers on one copy at a time: ceil(nnz *
+ * concurrency / w), w = min(num_workers, resident workers of the update kernel for (k,
+ * precision, lanes) on the current device), at least 4096.  0 (no copies) when
+ * concurrency <= 0, num_workers < 2 or nnz == 0. */
+int64_t cumf_hot_rows_per_copy(int64_t nnz, int32_t num_workers, int k, int precision, int lanes,
+                               float concurrency);
+
+/* Counts the ratings of every row and lays out the copies.  *out is freed with
+ * cumf_hot_rows_free.  Ids outside [0, m) x [0, n) are not counted. */
+int cumf_hot_rows_plan(const cumf_node *d_R, int64_t nnz, int32_t m, int32_t n, int64_t per_copy,
+                       int32_t max_copies, cumf_hot_rows **out, void *stream);
+/* Rows including the copies, and the number of rows that have copies (any may be NULL). */
+int cumf_hot_rows_info(const cumf_hot_rows *plan, int32_t *m_rows, int32_t *n_rows, int32_t *hot_m,
+                       int32_t *hot_n);
+/* Copies the plan's tables out (host or device buffers; NULL skips one): per row of P and
+ * of Q an int32 pair {copies, first extra row} (2*m and 2*n values; the second value of a
+ * row without copies is the row itself), and the ascending lists of rows with copies (hot_m
+ * and hot_n values).  Synchronous. */
+int cumf_hot_rows_tables(const cumf_hot_rows *plan, int32_t *tab_m, int32_t *tab_n, int32_t *grp_m,
+                         int32_t *grp_n);
+/* Rewrites each rating of a row with copies to name its copy (i mod copies; copy 0 is the row). */
+int cumf_hot_rows_assign(const cumf_hot_rows *plan, cumf_node *d_R, int64_t nnz, void *stream);
+/* Copies each row with copies into its extra rows (bitwise). */
+int cumf_hot_rows_spread(const cumf_hot_rows *plan, void *d_P, void *d_Q, int k, int precision,
+                         void *stream);
+/* Averages the copies of every row with copies and writes the mean to all of them. */
+int cumf_hot_rows_merge(const cumf_hot_rows *plan, void *d_P, void *d_Q, int k, int precision,
+                        void *stream);
+int cumf_hot_rows_free(cumf_hot_rows *plan);
 
 /* collect_data (singleGPU/sgd.cu:78-96) on the device: mean and population std of the
  * ratings, accumulated in fp64.  Results are written to host doubles. */

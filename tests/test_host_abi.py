@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol(lib):
     for name in names:
         assert hasattr(lib, name), name
     assert set(names) == set(_lib.exported_symbols())
-    assert lib.cumf_abi_version() == 1
+    assert lib.cumf_abi_version() == 2
 
 
 def test_default_params_match_reference(lib):
