@@ -93,12 +93,13 @@ def measured_peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the update kernel
-# at the c2 shape (one fp16 epoch, 100.86M samples, 29,184 workers), from one ncu capture of
-# this kernel with and without the copies of the most-rated rows.  Constants: ncu cannot run
-# inside the timed bench, and the captures are redone whenever the kernel changes.
-UPDATE_KERNEL_DRAM_BYTES_C2 = {True: 19.300e9, False: 18.400e9}  # keyed by "row copies in use"
-UPDATE_KERNEL_DRAM_BYTES_SOURCE = ("ncu capture of one c2 fp16 launch of sgd_hogwild_kernel<128,fp16,16> "
-                                   "(default row copies: 19.30 GB; --hot-rows 0: 18.40 GB)")
+# at the c2 shape in the default configuration (one fp16 epoch, 97,280 workers, 99.61M samples,
+# row copies, no L2 prefetch), from one ncu capture of this kernel.  A constant: ncu cannot run
+# inside the timed bench, and the capture is redone whenever the kernel or the defaults change;
+# other configurations report no traffic.
+UPDATE_KERNEL_DRAM_BYTES_C2 = 18.341e9
+UPDATE_KERNEL_DRAM_BYTES_SOURCE = ("ncu capture of one c2 fp16 launch of sgd_hogwild_kernel<128,fp16,16>, "
+                                   "97,280 workers, row copies, prefetch 0: 9.057 GB read + 9.284 GB written")
 
 
 class ClockSampler:
@@ -1039,7 +1040,7 @@ def main():
     def epoch(e):
         cm.sgd_update(d_R.data_ptr(), nnz, P.data_ptr(), m_rows, Q.data_ptr(), n_rows, K, prec, workers, args.lanes,
                       lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp,
-                      prefetch=args.prefetch, l2_hints=args.l2_hints, ring=args.ring)
+                      prefetch=args.prefetch, l2_hints=args.l2_hints, ring=args.ring, rows_copied=int(merges))
         if merges:
             hot.merge(P.data_ptr(), Q.data_ptr(), K, prec, sp)
 
@@ -1213,9 +1214,10 @@ def main():
                            "l2": "inputs larger than L2 (ratings 1.19 GB)", "parallelism": f"replicas{world}"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,
-                             "traffic": (UPDATE_KERNEL_DRAM_BYTES_C2[merges]
-                                         if (prec == "fp16" and args.scale >= 1.0 and not args.workers
-                                             and args.hot_rows in (None, 0.0, 0.5)) else None),
+                             "traffic": (UPDATE_KERNEL_DRAM_BYTES_C2
+                                         if (prec == "fp16" and args.scale >= 1.0 and not args.workers and merges
+                                             and args.hot_rows in (None, 0.5) and args.prefetch < 0
+                                             and args.lanes == 0) else None),
                              "traffic_source": UPDATE_KERNEL_DRAM_BYTES_SOURCE,
                              "bytes_per_sample": BYTES_PER_SAMPLE[prec]},
                 "l2_roofline": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,

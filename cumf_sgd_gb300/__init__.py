@@ -405,9 +405,10 @@ def sgd_update(d_R: int, nnz: int, d_P: int, m: int, d_Q: int, n: int, k: int, p
                num_workers: int, lanes: int, d_lr: int, first_epoch: int, n_epochs: int,
                lambda_p: float, lambda_q: float, seed: int, d_status: int = 0,
                stream: int = 0, prefetch: int = -1, l2_hints: int = -1, ring: int = -1,
-               freeze_q: int = 0) -> None:
+               freeze_q: int = 0, rows_copied: int = 0) -> None:
     """Batch-Hogwild epochs on caller-owned device buffers (sgd_kernel.cu:212-248)."""
-    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints, ring=ring, freeze_q=freeze_q)
+    t = _lib.Tuning(lanes=lanes, prefetch=prefetch, l2_hints=l2_hints, ring=ring, freeze_q=freeze_q,
+                    rows_copied=rows_copied)
     _lib.check(_lib.load().cumf_sgd_update_tuned(d_R, nnz, d_P, m, d_Q, n, k, PRECISIONS[precision],
                                                  num_workers, C.byref(t), d_lr, first_epoch, n_epochs,
                                                  lambda_p, lambda_q, seed, d_status or None,

@@ -51,7 +51,8 @@ class Params(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("prefetch", C.c_int32), ("l2_hints", C.c_int32),
-                ("ring", C.c_int32), ("freeze_q", C.c_int32), ("reserved_", C.c_int32 * 3)]
+                ("ring", C.c_int32), ("freeze_q", C.c_int32), ("rows_copied", C.c_int32),
+                ("reserved_", C.c_int32 * 2)]
 
 
 class Checkpoint(C.Structure):

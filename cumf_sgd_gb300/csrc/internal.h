@@ -58,6 +58,7 @@ struct Tuning {
     int hints = -1;     // -1 = default
     int ring = -1;      // -1 = default, 0 = register prefetch kernel, 1 = shared-memory ring kernel
     int freeze_q = 0;   // 1 = item rows are not written
+    int copies = 0;     // 1 = the ratings name copies of hot rows (default prefetch follows)
 };
 Tuning resolve_tuning(int k, int precision, Tuning t);
 int default_lanes(int k, int precision);

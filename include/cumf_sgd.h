@@ -120,14 +120,17 @@ typedef struct cumf_params {
 typedef struct cumf_tuning {
     int32_t lanes;         /* lanes per rating: 0 = default for (k, precision)           */
     int32_t prefetch;      /* rows of record j+prefetch are pulled into L2 during record j;
-                              -1 = default, 0 = off, at most 15                          */
+                              -1 = default (2; see rows_copied), 0 = off, at most 15      */
     int32_t l2_hints;      /* -1 = default, 0 = none, 1 = ratings evict_first and factor
                               rows evict_last                                            */
     int32_t ring;          /* -1 = default, 0 = one record's rows in flight per worker (held
                               in registers), 1 = four records' rows in flight, staged by
                               cp.async in a shared-memory ring                            */
     int32_t freeze_q;      /* 1 = update user rows only; item rows are read, never written  */
-    int32_t reserved_[3];
+    int32_t rows_copied;   /* 1 = the ratings name copies of the most-rated rows
+                              (cumf_hot_rows_assign): the default prefetch is then 0 unless
+                              P and Q together exceed twice the L2 size                     */
+    int32_t reserved_[2];
 } cumf_tuning;
 
 /* mf_model (singleGPU/sgd.h:110-138) as the model file holds it (main.cpp:247-266):
@@ -390,8 +393,10 @@ int cumf_dev_rmse_noalloc(const cumf_node *d_R, int64_t nnz, const float *d_P, i
  * README.md:61, scaled for the lane width in use). */
 int cumf_device_info(int gpu, int *sm_count, int *cc_major, int *cc_minor);
 int cumf_default_workers(int sm_count, int k, int precision, int lanes);
-/* Worker count for a problem of nnz ratings: three waves of resident workers (tail balance),
- * at most nnz/1024 so every worker has at least eight 128-record batches per epoch. */
+/* Worker count for a problem of nnz ratings: 3 to 16 whole waves of resident workers (tail
+ * balance), the count whose ceil(nnz / (W*128)) batches per worker overshoot nnz least, with
+ * at least eight 128-record batches per worker; problems too small for three such waves get
+ * nnz/1024 workers. */
 int cumf_auto_workers(int64_t nnz, int sm_count, int k, int precision, int lanes);
 
 /* glibc-compatible id shuffle used for bit-exact layout parity: fills map[0..size) with
