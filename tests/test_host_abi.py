@@ -55,6 +55,9 @@ def test_parse_argument_reference_semantics(lib):
     assert (b.param.ux, b.param.vy) == (4, 12) and b.model_path == "out.m"
     c = cm.parse_argument(["x", "--seed", "99", "--precision", "bf16sr", "-p", "te.bin", "tr"])
     assert c.param.seed == 99 and c.param.precision == "bf16sr" and c.va_path == "te.bin"
+    assert np.float32(c.param.hot_rows) == np.float32(0.5)  # copies of the most-rated rows by default
+    d = cm.parse_argument(["x", "--hot-rows", "0", "--deterministic", "3", "tr"])
+    assert d.param.hot_rows == 0 and d.param.deterministic == 3
 
 
 @pytest.mark.parametrize("argv,msg", [
@@ -63,6 +66,8 @@ def test_parse_argument_reference_semantics(lib):
     (["x", "-k", "abc", "tr"], "-k should be followed by a number"),
     (["x", "-s", "4"], "training data not specified"),
     (["x", "--precision", "fp8", "tr"], "unknown precision"),
+    (["x", "--hot-rows", "-1", "tr"], "--hot-rows should be 0 or more"),
+    (["x", "--hot-rows"], "need to specify a number after --hot-rows"),
 ])
 def test_parse_argument_errors(lib, argv, msg):
     with pytest.raises(ValueError, match=msg):
