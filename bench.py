@@ -609,6 +609,7 @@ def run_batched_suite(args, quiet=False):
     sm, _, _ = cm.device_info(0)
     rng = np.random.default_rng(4)
     nprob, epochs = 64, args.e2e_epochs
+    conc = args.hot_rows if getattr(args, "hot_rows", None) is not None else float(cm.Parameter().to_c().hot_rows)
     logu = lambda a, b: float(np.exp(rng.uniform(np.log(a), np.log(b))))
     probs = []
     t0 = time.time()
@@ -628,12 +629,23 @@ def run_batched_suite(args, quiet=False):
         d_R = torch.empty_like(d_raw)
         cm.dev_shuffle_scale(d_raw.data_ptr(), d_R.data_ptr(), nnz, pm.data_ptr(), m, qm.data_ptr(), n,
                              float(np.float32(1.0 / float(scale))))
-        P = torch.empty(m * k * 2, dtype=torch.uint8, device=dev)
-        Q = torch.empty(n * k * 2, dtype=torch.uint8, device=dev)
+        # Copies of the most-rated rows, planned as cumf_train plans them for this problem alone.
+        w = cm.auto_workers(nnz, sm, k, "fp16")
+        per_copy = cm.HotRows.per_copy(nnz, w, k, "fp16", 0, conc)
+        hot = cm.HotRows(d_R.data_ptr(), nnz, m, n, per_copy) if per_copy > 0 else None
+        if hot is not None and hot.hot_users + hot.hot_items == 0:
+            hot.close()
+            hot = None
+        if hot is not None:
+            hot.assign(d_R.data_ptr(), nnz)
+        mr, nr = (hot.m_rows, hot.n_rows) if hot else (m, n)
+        P = torch.empty(mr * k * 2, dtype=torch.uint8, device=dev)
+        Q = torch.empty(nr * k * 2, dtype=torch.uint8, device=dev)
         lr = torch.from_numpy(cm.lr_schedule(0.08, 0.3, 0.0, epochs + 4)).to(dev)
         probs.append(dict(m=m, n=n, nnz=nnz, k=k, d_R=d_R, P=P, Q=Q, pm=pm, qm=qm, lr=lr, scale=scale,
                           b=float(np.float32(mean) / np.float32(std)), lam=float(np.float32(0.05) / scale),
-                          te=torch.from_numpy(te.view(np.uint8)).to(dev), nte=len(te), seed=i))
+                          te=torch.from_numpy(te.view(np.uint8)).to(dev), nte=len(te), seed=i, hot=hot,
+                          m_rows=mr, n_rows=nr, workers=w))
     results = []
 
     def emit(d):
@@ -648,6 +660,8 @@ def run_batched_suite(args, quiet=False):
         for p in probs:
             cm.dev_init_factors(p["P"].data_ptr(), p["m"], p["k"], "fp16", p["seed"], 1)
             cm.dev_init_factors(p["Q"].data_ptr(), p["n"], p["k"], "fp16", p["seed"], 2)
+            if p["hot"] is not None:
+                p["hot"].spread(p["P"].data_ptr(), p["Q"].data_ptr(), p["k"], "fp16")
         torch.cuda.synchronize()
 
     def rmses():
@@ -663,26 +677,30 @@ def run_batched_suite(args, quiet=False):
         return np.array(out)
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # sequential plain launches
+    # sequential plain launches (each followed by the merge of that problem's row copies)
     init_all()
-    workers = [cm.auto_workers(p["nnz"], sm, p["k"], "fp16") for p in probs]
     e0.record()
     for e in range(epochs):
-        for p, w in zip(probs, workers):
-            cm.sgd_update(p["d_R"].data_ptr(), p["nnz"], p["P"].data_ptr(), p["m"], p["Q"].data_ptr(), p["n"],
-                          p["k"], "fp16", w, 0, p["lr"].data_ptr(), e, 1, p["lam"], p["lam"], p["seed"])
+        for p in probs:
+            cm.sgd_update(p["d_R"].data_ptr(), p["nnz"], p["P"].data_ptr(), p["m_rows"], p["Q"].data_ptr(),
+                          p["n_rows"], p["k"], "fp16", p["workers"], 0, p["lr"].data_ptr(), e, 1, p["lam"], p["lam"],
+                          p["seed"], rows_copied=int(p["hot"] is not None))
+            if p["hot"] is not None:
+                p["hot"].merge(p["P"].data_ptr(), p["Q"].data_ptr(), p["k"], "fp16")
     e1.record()
     torch.cuda.synchronize()
     seq_ms = e0.elapsed_time(e1)
     seq_rmse = rmses()
     total = sum(p["nnz"] for p in probs)
+    with_copies = sum(p["hot"] is not None for p in probs)
     emit({"arm": "64 sequential plain launches per epoch", "epochs": epochs, "ms": seq_ms,
-          "updates_per_sec": total * epochs / (seq_ms * 1e-3), "launches": epochs * nprob})
+          "updates_per_sec": total * epochs / (seq_ms * 1e-3), "launches": epochs * (nprob + with_copies),
+          "problems_with_row_copies": with_copies})
     # batched persistent launch
     init_all()
     batch = cm.Batch([dict(d_R=p["d_R"].data_ptr(), nnz=p["nnz"], d_P=p["P"].data_ptr(), m=p["m"], n=p["n"],
                            d_Q=p["Q"].data_ptr(), k=p["k"], lambda_p=p["lam"], lambda_q=p["lam"], seed=p["seed"],
-                           d_lr=p["lr"].data_ptr(), lr_len=epochs + 4) for p in probs])
+                           d_lr=p["lr"].data_ptr(), lr_len=epochs + 4, hot=p["hot"]) for p in probs])
     t0 = time.time()
     best = batch.autotune()
     tune_s = time.time() - t0
@@ -697,14 +715,16 @@ def run_batched_suite(args, quiet=False):
     assert batch.status() == 0
     bat_rmse = rmses()
     info = batch.info()
-    emit({"arm": "one graph-captured persistent launch", "epochs": epochs, "ms": bat_ms,
-          "updates_per_sec": total * epochs / (bat_ms * 1e-3), "launches": 1, "tuning": best,
+    emit({"arm": "one graph (one persistent launch per epoch with the merges when a problem has row copies)",
+          "epochs": epochs, "ms": bat_ms,
+          "updates_per_sec": total * epochs / (bat_ms * 1e-3), "graph_launches": 1, "tuning": best,
           "autotune_s": tune_s, "samples_per_epoch": info["samples_per_epoch"],
           "speedup_vs_sequential": seq_ms / bat_ms})
     emit({"event": "rmse", "sequential_mean": float(seq_rmse.mean()), "batched_mean": float(bat_rmse.mean()),
           "max_abs_diff": float(np.abs(seq_rmse - bat_rmse).max()),
           "per_problem": [[round(a, 4), round(b, 4)] for a, b in zip(seq_rmse, bat_rmse)]})
-    return {"problems": nprob, "total_nnz": total, "epochs": epochs, "sequential_ms": seq_ms,
+    return {"problems": nprob, "total_nnz": total, "epochs": epochs, "problems_with_row_copies": with_copies,
+            "sequential_ms": seq_ms,
             "batched_graph_ms": bat_ms, "speedup_vs_sequential": seq_ms / bat_ms,
             "batched_updates_per_sec": total * epochs / (bat_ms * 1e-3), "tuning": best, "autotune_s": tune_s,
             "mean_test_rmse_sequential": float(seq_rmse.mean()), "mean_test_rmse_batched": float(bat_rmse.mean()),
@@ -1021,6 +1041,9 @@ def main():
     per_copy = cm.HotRows.per_copy(nnz, workers, K, prec, args.lanes, conc)
     hot = cm.HotRows(d_R.data_ptr(), nnz, m, n, per_copy, stream=sp) if per_copy > 0 else None
     m_rows, n_rows = (hot.m_rows, hot.n_rows) if hot else (m, n)
+    # The ratings as the reference's kernel sees them (every rating names its own row), kept
+    # for the comparison run without copies after the timed region.
+    d_R_plain = d_R.clone() if (hot and rank == 0 and world == 1 and not args.no_extras) else None
     if hot:
         hot.assign(d_R.data_ptr(), nnz, sp)
     P = torch.empty(m_rows * K * eb, dtype=torch.uint8, device=dev)
@@ -1069,6 +1092,31 @@ def main():
     achieved = samples_per_launch * BYTES_PER_SAMPLE[prec] / launch_s / 1e9
     peak, peak_kind = measured_peaks()
     l2_gbs = l2_copy_gbs()
+
+    # The same epochs without row copies (each rating updates its own rows, as the reference's
+    # kernel does), default prefetch: untimed by the driver's contract, reported beside value.
+    plain = None
+    if d_R_plain is not None:
+        cm.dev_init_factors(P.data_ptr(), m, K, prec, rank, 1, sp)
+        cm.dev_init_factors(Q.data_ptr(), n, K, prec, rank, 2, sp)
+        def plain_epoch(e):
+            cm.sgd_update(d_R_plain.data_ptr(), nnz, P.data_ptr(), m, Q.data_ptr(), n, K, prec, workers, args.lanes,
+                          lr.data_ptr(), e % job_epochs, 1, lp, lp, rank, status.data_ptr(), sp,
+                          l2_hints=args.l2_hints, ring=args.ring)
+        for e in range(3):
+            plain_epoch(e)
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        p0.record(stream)
+        for e in range(3, 13):
+            plain_epoch(e)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        pms = p0.elapsed_time(p1) / 10
+        plain = {"updates_per_sec": nnz / (pms * 1e-3), "ms_per_epoch": pms, "workers": workers, "epochs_timed": 10,
+                 "what": "the same device-resident epochs without row copies (--hot-rows 0), default L2 prefetch"}
+        del d_R_plain
 
     hot_info = {"concurrency": conc, "per_copy": per_copy, "hot_users": hot.hot_users if hot else 0,
                 "hot_items": hot.hot_items if hot else 0,
@@ -1223,7 +1271,8 @@ def main():
                 "l2_roofline": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
                                 "peak_kind": "L2-resident copy (2 x 16 MB, 400 passes in one launch), measured in this run"},
                 "clocks": clocks, "e2e": e2e, "gpu_launches": args.steps * (2 if merges else 1), "cpu_baseline": cpu,
-                "cpu_port": cpu_port, "fp64_oracle": fp64, "value_w52": w52, "reference_kernel": refk,
+                "cpu_port": cpu_port, "fp64_oracle": fp64, "value_w52": w52, "value_without_copies": plain,
+                "reference_kernel": refk,
                 "time_to_target": ttt, "time_to_target_c1": ttt_c1, "batched": batched,
                 "precision_gap": precision_gap}
         print(json.dumps(line), flush=True)

@@ -617,14 +617,18 @@ def dev_strata_epochs(d_S: int, d_block_off: int, groups: int, d_P: int, m: int,
 class Batch:
     """Many independent factorizations in one persistent launch (cumf_batch_* in the C ABI).
     Each problem is a dict with device addresses d_R, d_P, d_Q, d_lr and m, n, nnz, k,
-    lambda_p, lambda_q, seed, lr_len and optionally num_workers."""
+    lambda_p, lambda_q, seed, lr_len and optionally num_workers and hot (a HotRows plan whose
+    assign and spread were applied; the batch merges its copies after every epoch)."""
 
     def __init__(self, problems):
         arr = (_lib.BatchProblem * len(problems))()
+        self._plans = [p.get("hot") for p in problems]  # the plans must outlive the batch
         for i, p in enumerate(problems):
+            hot = p.get("hot")
             arr[i] = _lib.BatchProblem(d_R=p["d_R"], nnz=p["nnz"], d_P=p["d_P"], m=p["m"], n=p["n"], d_Q=p["d_Q"],
                                        k=p["k"], num_workers=p.get("num_workers", 0), lambda_p=p["lambda_p"],
-                                       lambda_q=p["lambda_q"], seed=p["seed"], d_lr=p["d_lr"], lr_len=p["lr_len"])
+                                       lambda_q=p["lambda_q"], seed=p["seed"], d_lr=p["d_lr"], lr_len=p["lr_len"],
+                                       hot=hot._h.value if hot is not None else None)
         h = C.c_void_p()
         _lib.check(_lib.load().cumf_batch_create(arr, len(problems), C.byref(h)))
         self._h = h

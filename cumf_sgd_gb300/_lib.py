@@ -79,7 +79,7 @@ class BatchProblem(C.Structure):
     _fields_ = [("d_R", C.c_void_p), ("nnz", C.c_int64), ("d_P", C.c_void_p), ("m", C.c_int32), ("n", C.c_int32),
                 ("d_Q", C.c_void_p), ("k", C.c_int32), ("num_workers", C.c_int32), ("lambda_p", C.c_float),
                 ("lambda_q", C.c_float), ("seed", C.c_uint64), ("d_lr", C.c_void_p), ("lr_len", C.c_int32),
-                ("reserved_", C.c_int32)]
+                ("reserved_", C.c_int32), ("hot", C.c_void_p)]
 
 
 class BatchTuning(C.Structure):

@@ -8,6 +8,8 @@
 // barrier between epochs (as in the reference's persistent kernel).  The task table order is
 // chosen by the autotuner.  Each lane owns k/G consecutive halves of a row (4 to 32 B).
 // The launch (counter reset + kernel) can be captured in a CUDA graph and replayed.
+// Problems may carry copies of their most-rated rows (hot_rows.cu); the batch then runs one
+// launch per epoch and merges the copies between epochs, all inside the same graph.
 // Autotuning times candidate schedules (lanes per worker, blocks per SM, workers per
 // problem, task order) with an all-zero learning-rate table: the kernel then does the same loads and stores but
 // writes back the values it read (p + 0 = p, exactly representable), so the factors are
@@ -257,6 +259,7 @@ struct Batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_first = -1, graph_n = -1;
+    bool any_hot = false;  // a problem has row copies: one launch per epoch, merges between
     ~Batch() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -289,6 +292,12 @@ int batch_plan(Batch *b) {
         d.Q = p.d_Q;
         d.m = (uint32_t)p.m;
         d.n = (uint32_t)p.n;
+        if (p.hot) {  // ratings may name the copies' extra rows
+            int32_t hm, hn, mr, nr;
+            hot_rows_dims(p.hot, &hm, &hn, &mr, &nr);
+            d.m = (uint32_t)mr;
+            d.n = (uint32_t)nr;
+        }
         d.k = p.k;
         d.workers = w;
         d.batches = (int)batches_per_worker(p.nnz, w);
@@ -343,7 +352,7 @@ bool lanes_fit(const Batch *b, int lanes) {
     return true;
 }
 
-cudaError_t batch_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, cudaStream_t s) {
+cudaError_t kernel_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     const int bps = std::max(1, std::min(4, b->tuning.blocks_per_sm));
@@ -366,6 +375,23 @@ cudaError_t batch_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, 
     return cudaGetLastError();
 }
 
+// The epochs of one run: one persistent launch, or with row copies one launch per epoch,
+// each followed by the merge of every problem's copies (zero-learning-rate trials leave the
+// copies equal, so they need no merge).
+int batch_launch(Batch *b, bool zero_lr, int first_epoch, int n_epochs, cudaStream_t s) {
+    if (zero_lr || !b->any_hot) {
+        CUMF_CUDA(kernel_launch(b, zero_lr, first_epoch, n_epochs, s));
+        return CUMF_OK;
+    }
+    for (int ep = first_epoch; ep < first_epoch + n_epochs; ++ep) {
+        CUMF_CUDA(kernel_launch(b, false, ep, 1, s));
+        for (const cumf_batch_problem &p : b->probs)
+            if (p.hot)
+                if (int rc = cumf_hot_rows_merge(p.hot, p.d_P, p.d_Q, p.k, CUMF_FP16, s)) return rc;
+    }
+    return CUMF_OK;
+}
+
 }  // namespace
 
 }  // namespace cumf
@@ -385,10 +411,18 @@ int cumf_batch_create(const cumf_batch_problem *probs, int count, void **handle)
             return fail(CUMF_ERR_ARG, "batch_create: malformed problem " + std::to_string(i));
         if (p.num_workers > 0 && batches_per_worker(p.nnz, p.num_workers) * 4 > 0x7fffffffll)
             return fail(CUMF_ERR_ARG, "batch_create: too many batches per worker");
+        if (p.hot) {
+            int32_t hm, hn, mr, nr;
+            hot_rows_dims(p.hot, &hm, &hn, &mr, &nr);
+            if (hm != p.m || hn != p.n)
+                return fail(CUMF_ERR_ARG, "batch_create: row copies planned for another shape (problem " +
+                                              std::to_string(i) + ")");
+        }
         max_epoch_index = std::max(max_epoch_index, p.lr_len);
     }
     Batch *b = new Batch();
     b->probs.assign(probs, probs + count);
+    for (const cumf_batch_problem &p : b->probs) b->any_hot = b->any_hot || p.hot != nullptr;
     b->tuning.batches_target = 16;
     b->tuning.order = 2;
     b->tuning.blocks_per_sm = 4;
@@ -445,10 +479,7 @@ int cumf_batch_run(void *handle, int first_epoch, int n_epochs, int use_graph, v
         if (first_epoch + n_epochs > p.lr_len) return fail(CUMF_ERR_ARG, "batch_run: epochs beyond a problem's lr table");
     if (n_epochs == 0) return CUMF_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!use_graph) {
-        CUMF_CUDA(batch_launch(b, false, first_epoch, n_epochs, s));
-        return CUMF_OK;
-    }
+    if (!use_graph) return batch_launch(b, false, first_epoch, n_epochs, s);
     if (!b->exec || b->graph_first != first_epoch || b->graph_n != n_epochs) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         if (b->graph) cudaGraphDestroy(b->graph);
@@ -457,10 +488,11 @@ int cumf_batch_run(void *handle, int first_epoch, int n_epochs, int use_graph, v
         cudaStream_t cap;
         CUMF_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) e = batch_launch(b, false, first_epoch, n_epochs, cap);
+        int rc = e == cudaSuccess ? batch_launch(b, false, first_epoch, n_epochs, cap) : CUMF_OK;
         cudaError_t e2 = cudaStreamEndCapture(cap, &b->graph);
         cudaStreamDestroy(cap);
         if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+        if (rc != CUMF_OK) return rc;
         if (e2 != cudaSuccess) return cuda_fail(e2, "batch graph end capture");
         CUMF_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
         b->graph_first = first_epoch;
@@ -491,9 +523,9 @@ int cumf_batch_autotune(void *handle, void *stream, cumf_batch_tuning *best, dou
     auto trial = [&](const cumf_batch_tuning &cand) -> int {
         b->tuning = cand;
         if (int rc = batch_plan(b)) return rc;
-        CUMF_CUDA(batch_launch(b, true, 0, 1, s));  // warm-up
+        if (int rc = batch_launch(b, true, 0, 1, s)) return rc;  // warm-up
         CUMF_CUDA(cudaEventRecord(e0.e, s));
-        CUMF_CUDA(batch_launch(b, true, 0, 1, s));
+        if (int rc = batch_launch(b, true, 0, 1, s)) return rc;
         CUMF_CUDA(cudaEventRecord(e1.e, s));
         CUMF_CUDA(cudaEventSynchronize(e1.e));
         float ms = 0;

@@ -231,6 +231,13 @@ int64_t hot_rows_per_copy(int64_t nnz, int32_t num_workers, int k, int precision
     return std::max<int64_t>(kHotMinPerCopy, (int64_t)std::min(t, 9.0e18));
 }
 
+void hot_rows_dims(const cumf_hot_rows *h, int32_t *m, int32_t *n, int32_t *m_rows, int32_t *n_rows) {
+    *m = h->m;
+    *n = h->n;
+    *m_rows = h->m_rows;
+    *n_rows = h->n_rows;
+}
+
 }  // namespace cumf
 
 using namespace cumf;

@@ -144,6 +144,8 @@ constexpr float kHotDefaultConcurrency = 0.5f;
 // concurrency <= 0, fewer than two workers or no ratings).
 int64_t hot_rows_per_copy(int64_t nnz, int32_t num_workers, int k, int precision, int lanes, float concurrency,
                           int sm_count);
+// Rows of a plan before (m, n) and with (m_rows, n_rows) the copies.
+void hot_rows_dims(const cumf_hot_rows *h, int32_t *m, int32_t *n, int32_t *m_rows, int32_t *n_rows);
 // Size in bytes of one factor element for a precision.
 inline int elem_bytes(int precision) { return precision == CUMF_FP32 ? 4 : 2; }
 

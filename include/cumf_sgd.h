@@ -511,7 +511,11 @@ int cumf_train_ckpt(const cumf_problem *tr, const cumf_problem *te, const cumf_p
 /* ---- batched factorizations (no reference counterpart) ------------------------------ */
 /* One problem of a batch: device ratings with ids in range and ratings already scaled, fp16
  * factors P (m x k) and Q (n x k), k in {32, 64, 128}; num_workers 0 = set by the batch
- * tuning; d_lr has lr_len learning rates (epoch index < lr_len). */
+ * tuning; d_lr has lr_len learning rates (epoch index < lr_len).  hot: copies of the
+ * problem's most-rated rows (a cumf_hot_rows_plan of these m x n, cumf_hot_rows_assign
+ * already applied to d_R, P and Q allocated with the plan's m_rows and n_rows rows and
+ * spread), or NULL.  With any copies in the batch, cumf_batch_run launches one epoch at a
+ * time and merges the copies after each (the launches stay in one graph). */
 typedef struct cumf_batch_problem {
     const cumf_node *d_R;
     int64_t nnz;
@@ -526,6 +530,7 @@ typedef struct cumf_batch_problem {
     const float *d_lr;
     int32_t lr_len;
     int32_t reserved_;
+    const cumf_hot_rows *hot;
 } cumf_batch_problem;
 
 /* Schedule of a batched launch: workers per problem so each has about batches_target
@@ -546,9 +551,10 @@ int cumf_batch_create(const cumf_batch_problem *probs, int count, void **batch);
 int cumf_batch_destroy(void *batch);
 int cumf_batch_set_tuning(void *batch, const cumf_batch_tuning *tuning);
 int cumf_batch_get_info(void *batch, cumf_batch_tuning *tuning, int *tasks_per_epoch, int64_t *samples_per_epoch);
-/* Epochs [first_epoch, first_epoch + n_epochs) of every problem in one persistent launch;
- * use_graph = 1 captures the launch (counter reset + kernel) in a CUDA graph on first use and
- * replays it while (first_epoch, n_epochs) and the tuning stay the same. */
+/* Epochs [first_epoch, first_epoch + n_epochs) of every problem in one persistent launch
+ * (one launch per epoch, each followed by the merges, when a problem has row copies);
+ * use_graph = 1 captures the launches (counter reset + kernel [+ merges]) in a CUDA graph on
+ * first use and replays it while (first_epoch, n_epochs) and the tuning stay the same. */
 int cumf_batch_run(void *batch, int first_epoch, int n_epochs, int use_graph, void *stream);
 /* CUMF_ERR_RANGE if any launch met an out-of-range index (such ratings are skipped). */
 int cumf_batch_status(void *batch, int *status);

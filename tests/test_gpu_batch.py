@@ -132,3 +132,48 @@ def test_batched_tuning_refuses_lanes_a_problem_cannot_take(lib, cuda):
     with pytest.raises(RuntimeError):
         b.set_tuning(16, 2, 4, lanes=12)
     assert b.info()["lanes"] == 16
+
+
+def test_batched_row_copies_single_worker_bit_exact(lib, orc, cuda):
+    """Problems with copies of their most-rated rows (at least 40 ratings per copy): the batch
+    runs one launch per epoch and merges the copies after each.  One worker per problem: the
+    extended factors equal the oracle's epochs over the rewritten ratings, each followed by
+    the restated merge, bit for bit (copies included)."""
+    import torch
+    from oracle import hot_rows_oracle as ho
+    probs, host, lr, _keep = make(cuda, 2)
+    plans = []
+    for p, h in zip(probs, host):
+        plan = cm.HotRows(p["d_R"], p["nnz"], h["m"], h["n"], 40)
+        plan.assign(p["d_R"], p["nnz"])
+        P = torch.empty(plan.m_rows * h["k"] * 2, dtype=torch.uint8, device=cuda)
+        Q = torch.empty(plan.n_rows * h["k"] * 2, dtype=torch.uint8, device=cuda)
+        cm.dev_init_factors(P.data_ptr(), h["m"], h["k"], "fp16", h["seed"], 1)
+        cm.dev_init_factors(Q.data_ptr(), h["n"], h["k"], "fp16", h["seed"], 2)
+        plan.spread(P.data_ptr(), Q.data_ptr(), h["k"], "fp16")
+        h.update(P=P, Q=Q, plan=plan)
+        p.update(d_P=P.data_ptr(), d_Q=Q.data_ptr(), hot=plan)
+        plans.append(plan)
+    assert sum(pl.hot_users + pl.hot_items for pl in plans) > 0
+    b = cm.Batch(probs)
+    b.set_tuning(16, 2, 4, lanes=16)
+    b.run(0, 2, use_graph=True)
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    for h in host:
+        plan = h["plan"]
+        tm, tn, gm, gn = plan.tables()
+        want = ho.plan(h["rec"], h["m"], h["n"], 40)
+        rec = ho.assign(h["rec"], want)
+        P = np.zeros((plan.m_rows, h["k"]), np.float32)
+        Q = np.zeros((plan.n_rows, h["k"]), np.float32)
+        P[:h["m"]] = orc.init_factors(h["m"], h["k"], "fp16", h["seed"], 1)
+        Q[:h["n"]] = orc.init_factors(h["n"], h["k"], "fp16", h["seed"], 2)
+        ho.spread(P, tm, gm)
+        ho.spread(Q, tn, gn)
+        for ep in range(2):
+            orc.sgd_epochs(rec, P, Q, "fp16", 1, lr, ep, 1, 0.05, 0.04, h["seed"], lanes=16)
+            ho.merge(P, tm, gm, "fp16")
+            ho.merge(Q, tn, gn, "fp16")
+        np.testing.assert_array_equal(as_f32(h["P"], plan.m_rows, h["k"]), P)
+        np.testing.assert_array_equal(as_f32(h["Q"], plan.n_rows, h["k"]), Q)
