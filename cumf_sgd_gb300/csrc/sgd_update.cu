@@ -580,9 +580,11 @@ int resident_workers(int k, int precision, int lanes, int sm_count) {
     return resident_workers_of(e, kDefaultRing != 0, sm_count);
 }
 
-// With the hot rows split into copies the kernel is issue-bound while P and Q stay mostly
-// in L2, and the prefetch instructions cost more than they save (c2, 480,189 x 17,770, per
-// epoch: fp16 9.03 against 9.69 ms, fp32 18.2 against 19.9, bf16-SR 20.0 against 20.8); with
+// With the hot rows split into copies, or with the item rows frozen (fold-in epochs), no
+// worker queues on a hot row's lines: the kernel is issue-bound while P and Q stay mostly in
+// L2, and the prefetch instructions cost more than they save (c2, 480,189 x 17,770, per
+// epoch: fp16 9.03 against 9.69 ms, fp32 18.2 against 19.9, bf16-SR 20.0 against 20.8; a
+// 5.2M-rating fold-in epoch: fp16 0.76 against 0.85 ms, bf16-SR 1.31 against 1.37); with
 // factors far beyond L2 the row loads go to DRAM and the prefetch pays again (c3, 1,000,990 x
 // 624,961, 416 MB of fp16 factors: 28.2 ms with it against 31.4 without).
 static int copies_prefetch(int32_t m, int32_t n, int k, int precision) {
@@ -610,7 +612,7 @@ cudaError_t launch_sgd_update(const cumf_node *d_R, int64_t nnz, void *d_P, int3
                               int n_epochs, float lambda_p, float lambda_q, uint64_t seed,
                               int *d_status, cudaStream_t stream, int *lanes_used) {
     Tuning t = resolve_tuning(k, precision, tuning);
-    if (tuning.prefetch < 0 && tuning.copies) t.prefetch = copies_prefetch(m, n, k, precision);
+    if (tuning.prefetch < 0 && (tuning.copies || tuning.freeze_q)) t.prefetch = copies_prefetch(m, n, k, precision);
     const KernelEntry *e = find_kernel(k, precision, t.lanes);
     if (!e) return cudaErrorInvalidValue;
     if (lanes_used) *lanes_used = e->lanes;

@@ -128,8 +128,9 @@ typedef struct cumf_tuning {
                               cp.async in a shared-memory ring                            */
     int32_t freeze_q;      /* 1 = update user rows only; item rows are read, never written  */
     int32_t rows_copied;   /* 1 = the ratings name copies of the most-rated rows
-                              (cumf_hot_rows_assign): the default prefetch is then 0 unless
-                              P and Q together exceed twice the L2 size                     */
+                              (cumf_hot_rows_assign).  With rows_copied or freeze_q the
+                              default prefetch is 0 unless P and Q together exceed twice the
+                              L2 size                                                      */
     int32_t reserved_[2];
 } cumf_tuning;
 
