@@ -226,3 +226,22 @@ def test_checkpoint_arguments_without_gpu(lib, tmp_path):
     exe = os.path.join(ROOT, "cumf_sgd_gb300", "bin", "cumf_sgd")
     res = subprocess.run([exe, "--resume", "train.bin"], capture_output=True, text=True)
     assert res.returncode == 1 and "--checkpoint" in res.stdout
+
+
+def test_hot_rows_api_refuses_bad_arguments_without_a_gpu(lib):
+    """The copies' entry points check their arguments before touching a device."""
+    import ctypes as C
+    out = C.c_void_p()
+    assert lib.cumf_hot_rows_plan(None, 10, 5, 5, 100, 8, None, None) != 0  # no output pointer
+    for args in ((None, -1, 5, 5, 100, 8), (None, 10, 0, 5, 100, 8), (None, 10, 5, 5, 0, 8), (None, 10, 5, 5, 100, 0),
+                 (None, 10, 5, 5, 100, 8)):  # the last: ratings without a pointer
+        assert lib.cumf_hot_rows_plan(*args, C.byref(out), None) != 0
+        assert out.value is None
+    assert lib.cumf_hot_rows_info(None, None, None, None, None) != 0
+    assert lib.cumf_hot_rows_assign(None, None, 0, None) != 0
+    assert lib.cumf_hot_rows_merge(None, None, None, 128, 0, None) != 0
+    assert lib.cumf_hot_rows_free(None) == 0
+    # no copies for one worker, no ratings or a concurrency of 0
+    assert lib.cumf_hot_rows_per_copy(10**8, 1, 128, 0, 0, 0.5) == 0
+    assert lib.cumf_hot_rows_per_copy(0, 1000, 128, 0, 0, 0.5) == 0
+    assert lib.cumf_hot_rows_per_copy(10**8, 1000, 128, 0, 0, 0.0) == 0
