@@ -12,11 +12,13 @@
 //   forward   H1 = gelu(X W1^T + b1), H2 = gelu(H1 W2^T + b2), Y = H2 W3^T + b3
 //   backward  dW = dZ^T A  ->  (dZ^T)(A^T)^T on transposed copies; dA = dZ W -> dZ (W^T)^T
 // Loss: mean over rows of the squared error summed over the output dimension.
+#include <cub/cub.cuh>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -75,6 +77,134 @@ __global__ void user_qsum_kernel(const cumf_node *R, int64_t nnz, int32_t m, int
             }
         } else {
             for (int j = lane; j < k; j += 32) atomicAdd(dst + j, c * q[j]);
+        }
+    }
+}
+
+// Stream-ordered scratch of the feature extraction from a pool of this library that keeps up
+// to 256 MB between calls (the default pool returns its memory at every synchronisation, and
+// mapping it again cost more than the feature kernels at 50,000 users).
+cudaError_t feature_scratch(void **p, size_t bytes, cudaStream_t s) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props;
+            memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            if ((e = cudaMemPoolCreate(&pools[dev], &props)) != cudaSuccess) return e;
+            uint64_t keep = 256ull << 20;
+            if ((e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+                return e;
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+// Sort keys of the ratings: the user, or m for a rating outside [0, m) x [0, n) (sorted last
+// and left out); values: the rating's index.
+__global__ void user_keys_kernel(const cumf_node *R, uint32_t nnz, int32_t m, int32_t n, uint32_t *key,
+                                 uint32_t *idx) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += gridDim.x * blockDim.x) {
+        const cumf_node x = R[i];
+        const bool ok = (uint32_t)x.u < (uint32_t)m && (uint32_t)x.v < (uint32_t)n;
+        key[i] = ok ? (uint32_t)x.u : (uint32_t)m;
+        idx[i] = i;
+    }
+}
+
+// seg[u] = the first sorted position whose key is >= u, u = 0..m (binary search).
+__global__ void user_segments_kernel(const uint32_t *key, uint32_t nnz, int32_t m, int64_t *seg) {
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u <= m; u += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = nnz;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (key[mid] < (uint32_t)u) lo = mid + 1;
+            else hi = mid;
+        }
+        seg[u] = lo;
+    }
+}
+
+// One warp per user over the user's ratings in their original order (a stable sort by user):
+// the rating sum and sum of squares by a fixed-order warp reduction, then
+// sum (r - mean) q / deg accumulated rating by rating in registers, 32 * KPL columns per
+// pass; X[u] = (that sum, log(1 + deg)/4, (mean - 3)/2, var/2).  The ratings are fetched 32
+// at a time (one per lane, then broadcast) and the item rows of four ratings are loaded
+// before they are added, in rating order.  No atomics: the features are the same bits on
+// every run.
+template <int KPL>
+__global__ void user_rows_kernel(const cumf_node *R, const uint32_t *order, const int64_t *seg, int32_t m,
+                                 const float *Q, int k, float *X, int ldx) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = w0; u < m; u += nw) {
+        const int64_t a = seg[u], b = seg[u + 1];
+        float s = 0.f, s2 = 0.f;
+        for (int64_t t = a + lane; t < b; t += 32) {
+            const float r = R[order[t]].r;
+            s += r;
+            s2 += r * r;
+        }
+        for (int o = 16; o >= 1; o >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        const float d = (float)(b - a);
+        const float mean = d > 0 ? s / d : 0.f;
+        float *xu = X + u * ldx;
+        for (int c0 = 0; c0 < k; c0 += 32 * KPL) {
+            float acc[KPL];
+#pragma unroll
+            for (int j = 0; j < KPL; ++j) acc[j] = 0.f;
+            bool col[KPL];
+#pragma unroll
+            for (int j = 0; j < KPL; ++j) col[j] = c0 + lane + 32 * j < k;
+            for (int64_t t0 = a; t0 < b; t0 += 32) {
+                float cl = 0.f;
+                int vl = 0;
+                if (t0 + lane < b) {
+                    const cumf_node x = R[order[t0 + lane]];
+                    cl = (x.r - s / d) / d;
+                    vl = x.v;
+                }
+                const int cnt = (int)(b - t0 < 32 ? b - t0 : 32);
+                for (int j0 = 0; j0 < cnt; j0 += 4) {
+                    float c4[4], q4[4][KPL];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        c4[h] = __shfl_sync(0xffffffffu, cl, (j0 + h) & 31);
+                        const int v = __shfl_sync(0xffffffffu, vl, (j0 + h) & 31);
+                        const float *q = Q + (int64_t)v * k + c0 + lane;
+#pragma unroll
+                        for (int j = 0; j < KPL; ++j) q4[h][j] = (j0 + h < cnt && col[j]) ? q[32 * j] : 0.f;
+                    }
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                        if (j0 + h < cnt) {
+#pragma unroll
+                            for (int j = 0; j < KPL; ++j) acc[j] += c4[h] * q4[h][j];
+                        }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < KPL; ++j)
+                if (col[j]) xu[c0 + lane + 32 * j] = acc[j];
+        }
+        if (lane == 0) {
+            xu[k] = logf(1.f + d) * 0.25f;
+            xu[k + 1] = d > 0 ? (mean - 3.f) * 0.5f : 0.f;
+            xu[k + 2] = (d > 0 ? fmaxf(s2 / d - mean * mean, 0.f) : 0.f) * 0.5f;
         }
     }
 }
@@ -721,8 +851,51 @@ int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int3
     if (!d_Q || !d_X || m <= 0 || n <= 0 || k <= 0 || nnz < 0 || (nnz > 0 && !d_R))
         return fail(CUMF_ERR_ARG, "user_features: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    // One stream-ordered scratch: the centred mean accumulates in k-wide rows (16-byte aligned
-    // for the vector atomics), then degree, rating sum and sum of squares per user.
+    if (nnz < 0xffffffffll && m < 0x7fffffff) {
+        // The ratings stably sorted by user (32-bit keys and indices), then one warp per user.
+        const uint32_t N = (uint32_t)nnz;
+        int end_bit = 1;
+        while (end_bit < 32 && ((uint32_t)m >> end_bit) != 0) ++end_bit;
+        size_t tmp_bytes = 0;
+        CUMF_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                                  (const uint32_t *)nullptr, (uint32_t *)nullptr, N, 0, end_bit, s));
+        auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t kb = up((size_t)N * 4 + 4), sb = up(((size_t)m + 1) * 8);
+        void *buf = nullptr;
+        CUMF_CUDA(feature_scratch(&buf, 4 * kb + sb + up(tmp_bytes), s));
+        char *p = static_cast<char *>(buf);
+        uint32_t *key = reinterpret_cast<uint32_t *>(p), *idx = reinterpret_cast<uint32_t *>(p + kb);
+        uint32_t *key2 = reinterpret_cast<uint32_t *>(p + 2 * kb), *idx2 = reinterpret_cast<uint32_t *>(p + 3 * kb);
+        int64_t *seg = reinterpret_cast<int64_t *>(p + 4 * kb);
+        void *tmp = p + 4 * kb + sb;
+        cudaError_t e = cudaSuccess;
+        if (N > 0) {
+            user_keys_kernel<<<grid_of(N), kT, 0, s>>>(d_R, N, m, n, key, idx);
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key, key2, idx, idx2, N, 0, end_bit, s);
+        }
+        if (e == cudaSuccess) {
+            user_segments_kernel<<<grid_of((int64_t)m + 1), kT, 0, s>>>(key2, N, m, seg);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            const int g = grid_of((int64_t)m * 32);
+            if (k <= 32) user_rows_kernel<1><<<g, kT, 0, s>>>(d_R, idx2, seg, m, d_Q, k, d_X, k + 3);
+            else if (k <= 64) user_rows_kernel<2><<<g, kT, 0, s>>>(d_R, idx2, seg, m, d_Q, k, d_X, k + 3);
+            else if (k <= 128) user_rows_kernel<4><<<g, kT, 0, s>>>(d_R, idx2, seg, m, d_Q, k, d_X, k + 3);
+            else user_rows_kernel<8><<<g, kT, 0, s>>>(d_R, idx2, seg, m, d_Q, k, d_X, k + 3);
+            e = cudaGetLastError();
+        }
+        const cudaError_t ef = cudaFreeAsync(buf, s);
+        CUMF_CUDA(e);
+        CUMF_CUDA(ef);
+        CUMF_CUDA(cudaStreamSynchronize(s));
+        return CUMF_OK;
+    }
+    // 2^32 ratings or more: vector atomics into per-user rows.  One stream-ordered scratch: the
+    // centred mean accumulates in k-wide rows (16-byte aligned for the vector atomics), then
+    // degree, rating sum and sum of squares per user.
     const size_t acc_bytes = (size_t)m * k * 4, scratch = acc_bytes + 3 * (size_t)m * 4;
     void *buf = nullptr;
     CUMF_CUDA(cudaMallocAsync(&buf, scratch, s));

@@ -420,9 +420,12 @@ int cumf_grid_problem(cumf_node *R, int64_t nnz, int32_t m, int32_t n, int ux, i
 int cumf_tc_gemm(const void *d_A, const void *d_B, int M, int N, int K, const float *d_bias, int act,
                  void *d_out, int out_f32, int ldo, float *d_pre, int *d_status, void *stream);
 
-/* User features for the warm start, from ratings with ids already in [0,m) x [0,n) and fp32
- * item factors Q (n x k): d_X (m x (k+3)) = [sum_i (r_ui - mean_u) q_i / deg_u,
- * log(1+deg_u)/4, (mean_u - 3)/2, var_u/2]; users without ratings get zeros. */
+/* User features for the warm start, from ratings and fp32 item factors Q (n x k): d_X
+ * (m x (k+3)) = [sum_i (r_ui - mean_u) q_i / deg_u, log(1+deg_u)/4, (mean_u - 3)/2,
+ * var_u/2]; users without ratings get zeros, ratings outside [0,m) x [0,n) are left out.
+ * Below 2^32 ratings the sums run in each user's rating order (a stable sort by user), so
+ * every call gives the same bits; the scratch comes from a pool of the library that keeps
+ * up to 256 MB per device between calls. */
 int cumf_user_features(const cumf_node *d_R, int64_t nnz, const float *d_Q, int32_t n, int k, int32_t m,
                        float *d_X, void *stream);
 

@@ -62,23 +62,38 @@ def test_mlp_training_fits_a_smooth_map(lib, cuda):
     assert after < 0.1 * before, (before, after)
 
 
-def test_user_features_match_fp64(lib, cuda):
+@pytest.mark.parametrize("k", [128, 96, 300])
+def test_user_features_match_fp64(lib, cuda, k):
+    """Against the float64 restatement (k = 96 and 300: a partial last column pass); every
+    call gives the same bits; ratings outside the matrix are left out."""
     import torch
     rng = np.random.default_rng(5)
-    m, n, k, nnz = 500, 200, 128, 20000
+    m, n, nnz = 500, 200, 20000
     rec = np.empty(nnz, dtype=cm.NODE_DTYPE)
     rec["u"] = rng.integers(0, m - 10, nnz)  # the last users have no ratings
     rec["v"] = rng.integers(0, n, nnz)
     rec["r"] = rng.integers(1, 6, nnz).astype(np.float32)
+    rec["u"][:300] = rng.integers(0, 40, 300)  # a few users with many ratings
     Q = (rng.standard_normal((n, k)) * 0.3).astype(np.float32)
-    dR = torch.from_numpy(rec.view(np.uint8).copy()).to(cuda)
     dQ = torch.from_numpy(Q).to(cuda)
-    dX = torch.empty(m, k + 3, device=cuda)
-    cm.user_features(dR.data_ptr(), nnz, dQ.data_ptr(), n, k, m, dX.data_ptr())
-    got = dX.cpu().numpy()
+
+    def feats(records):
+        dR = torch.from_numpy(records.view(np.uint8).copy()).to(cuda)
+        dX = torch.empty(m, k + 3, device=cuda)
+        cm.user_features(dR.data_ptr(), len(records), dQ.data_ptr(), n, k, m, dX.data_ptr())
+        return dX.cpu().numpy()
+
+    got = feats(rec)
     ref = mlp_oracle.user_features(rec, Q, m, k)
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
     assert (got[-10:] == 0).all()
+    assert (feats(rec) == got).all()  # deterministic
+    bad = np.empty(7, dtype=cm.NODE_DTYPE)
+    bad["u"] = [-1, m, 3, 5, m + 7, 2, 0]
+    bad["v"] = [1, 1, -2, n, 0, n + 1, -5]
+    bad["r"] = 4.0
+    mixed = np.concatenate([bad[:3], rec[:nnz // 2], bad[3:], rec[nnz // 2:]])
+    assert (feats(mixed) == got).all()  # out-of-range ratings change nothing
 
 
 def test_mlp_training_with_a_short_last_batch_continues_across_calls(lib, cuda):
