@@ -146,3 +146,20 @@ def test_checkpoint_records_copies(lib, cuda, tmp_path):
     with pytest.raises(cm.CumfError, match="hot_rows"):
         cm.sgd_train_ckpt(prob, None, cm.Parameter(**{**par.__dict__, "hot_rows": 2.0}), path, every=1,
                           resume=True)
+
+
+def test_per_epoch_rmse_and_persistent_launches_with_copies(lib, cuda):
+    """With copies, the per-epoch test RMSE (evaluated after each epoch's merge) ends at the
+    returned model's RMSE; several epochs per launch (merges after each launch) still train."""
+    spec = synth.scaled(synth.C2, 0.02)
+    train, test = synth.generate(spec, seed=1)
+    prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n)
+    te = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
+    par = cm.Parameter(k=128, num_workers=0, num_iters=6, alpha=0.08, beta=0.3, seed=2, gpu=0, quiet=1)
+    model, st, rm, _ = cm.sgd_train_ex(prob, te, par)
+    assert st.hot_items > 0
+    assert abs(rm[-1] - cm.calc_rmse(te, model)) <= 1e-6 and rm[-1] < rm[0]
+    par3 = cm.Parameter(**{**par.__dict__, "num_workers": 2048, "epochs_per_launch": 3})
+    m3, st3 = cm.sgd_train(prob, None, par3, with_stats=True)
+    assert st3.hot_items > 0 and np.isfinite(m3.P).all()
+    assert cm.calc_rmse(te, m3) < rm[0]
