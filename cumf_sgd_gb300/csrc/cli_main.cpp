@@ -12,8 +12,8 @@
 // --checkpoint writes the in-HBM factors every N epochs (default 1; mode A only) and
 // --resume continues from a matching checkpoint (cumf_train_ckpt).  --deterministic 1 (or a
 // grid size G) trains with the bit-reproducible stratified schedule instead of batch-Hogwild.
-// --hot-rows X sets the expected workers per copy of a most-rated row (0: no copies, every
-// rating updates its own row as in the reference).
+// --hot-rows X gives the most-rated rows copies for about X workers each (0.5 suits skewed
+// item popularity; the default 0 keeps the reference's update, one row per rating).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>

@@ -111,8 +111,9 @@ typedef struct cumf_params {
     int64_t tail_start;    /* (tail_epochs) [tail_start, nnz) (e.g. newly added users'
                               ratings): those epochs update user rows only (item rows frozen) */
     float hot_rows;        /* batch-Hogwild, mode A: copies of the most-rated rows
-                              (cumf_hot_rows_*) for this many expected workers per copy;
-                              0 = none (every rating updates its own row, as the reference) */
+                              (cumf_hot_rows_*) for this many expected workers per copy
+                              (0.5 suits skewed item popularity); 0 = none, the default
+                              (every rating updates its own row, as the reference)        */
     int32_t reserved_[3];
 } cumf_params;
 
@@ -177,7 +178,7 @@ typedef struct cumf_args {
 int cumf_abi_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 const char *cumf_last_error(void);
-/* Reference defaults (singleGPU/sgd.h:45) plus seed 0, FP16, auto lanes, hot_rows 0.5. */
+/* Reference defaults (singleGPU/sgd.h:45) plus seed 0, FP16, auto lanes, hot_rows 0 (no copies). */
 int cumf_default_params(cumf_params *p);
 /* parse_argument (singleGPU/main.cpp:33-227): same flags, same -s rounding, the same
  * default model path (<basename of train file>.model), u*v==1 forces x=y=1.  Long flags
@@ -316,7 +317,7 @@ int cumf_sgd_update_tuned(const cumf_node *d_R, int64_t nnz, void *d_P, int32_t 
  * Use: plan on the shuffled, scaled ratings; allocate P and Q with m_rows and n_rows rows;
  * assign (rewrites the ratings' ids in place); init the first m / n rows; spread; then
  * cumf_sgd_update(..., m_rows, ..., n_rows, ...) and merge after every call.
- * cumf_train does this when params.hot_rows > 0. */
+ * cumf_train does this when params.hot_rows > 0 (off by default). */
 typedef struct cumf_hot_rows cumf_hot_rows;
 
 /* Ratings per copy for `concurrency` expected workers on one copy at a time: ceil(nnz *

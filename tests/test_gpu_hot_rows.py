@@ -112,12 +112,13 @@ def _train(train, test, spec, **kw):
 
 def test_train_with_copies_keeps_quality(lib, cuda):
     """5M ratings of the 480,189 x 17,770 family scaled by 1/20 (Zipf item popularity):
-    automatic workers, 20 epochs.  The default copies cover the most-rated items; the test
-    RMSE is no worse than without copies (bound 0.002), and the model has the plain shapes."""
+    automatic workers, 20 epochs.  Copies (hot_rows 0.5) cover the most-rated items; the test
+    RMSE is no worse than without copies, the default (bound 0.002), and the model has the
+    plain shapes."""
     spec = synth.scaled(synth.C2, 0.05)
     train, test = synth.generate(spec, seed=0)
-    rm_hot, st_hot, model = _train(train, test, spec)
-    rm_plain, st_plain, _ = _train(train, test, spec, hot_rows=0)
+    rm_hot, st_hot, model = _train(train, test, spec, hot_rows=0.5)
+    rm_plain, st_plain, _ = _train(train, test, spec)
     assert st_hot.hot_items > 0 and st_hot.extra_rows > 0
     assert st_plain.hot_items == 0 and st_plain.hot_users == 0 and st_plain.extra_rows == 0
     assert model.P.shape == (spec.m, 128) and model.Q.shape == (spec.n, 128)
@@ -155,7 +156,8 @@ def test_per_epoch_rmse_and_persistent_launches_with_copies(lib, cuda):
     train, test = synth.generate(spec, seed=1)
     prob = cm.MFProblem.from_arrays(train["u"], train["v"], train["r"], m=spec.m, n=spec.n)
     te = cm.MFProblem.from_arrays(test["u"], test["v"], test["r"])
-    par = cm.Parameter(k=128, num_workers=0, num_iters=6, alpha=0.08, beta=0.3, seed=2, gpu=0, quiet=1)
+    par = cm.Parameter(k=128, num_workers=0, num_iters=6, alpha=0.08, beta=0.3, seed=2, gpu=0, quiet=1,
+                       hot_rows=0.5)
     model, st, rm, _ = cm.sgd_train_ex(prob, te, par)
     assert st.hot_items > 0
     assert abs(rm[-1] - cm.calc_rmse(te, model)) <= 1e-6 and rm[-1] < rm[0]

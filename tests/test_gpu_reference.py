@@ -45,15 +45,15 @@ def ref_tools():
     return ref_tools
 
 
-def _ours(train_path, model_path, workers, seed):
+def _ours(train_path, model_path, workers, seed, extra=()):
     import subprocess
     from oracle import ref_tools
-    cmd = [CLI] + ref_tools.cumf_flags(workers, 20) + ["--seed", str(seed), "--quiet", train_path, model_path]
+    cmd = [CLI] + ref_tools.cumf_flags(workers, 20) + ["--seed", str(seed), "--quiet", *extra, train_path, model_path]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-500:] + r.stderr[-500:]
 
 
-def _compare(ref_tools, spec, tmp_path, reps):
+def _compare(ref_tools, spec, tmp_path, reps, extra=()):
     sm, _, _ = cm.device_info(0)
     workers = 52 * sm
     train, test = synth.generate(spec, seed=0, device="cuda")
@@ -75,13 +75,15 @@ def _compare(ref_tools, spec, tmp_path, reps):
         assert out["rc"] == 0 and out["update_per_sec"], out
         ref.append(score(mp))
         mo = str(tmp_path / "ours.model")
-        _ours(tr_path, mo, workers, rep + 1)
+        _ours(tr_path, mo, workers, rep + 1, extra)
         ours.append(score(mo))
     return float(np.mean(ref)), float(np.mean(ours)), ref, ours
 
 
-def test_hogwild_c2_shape_within_0002_of_reference_kernel(ref_tools, lib, cuda, tmp_path):
-    ref, ours, r_all, o_all = _compare(ref_tools, synth.C2, tmp_path, reps=1)
+@pytest.mark.parametrize("extra", [(), ("--hot-rows", "0.5")], ids=["plain", "row-copies"])
+def test_hogwild_c2_shape_within_0002_of_reference_kernel(ref_tools, lib, cuda, tmp_path, extra):
+    """The default update and the copies of the most-rated rows (--hot-rows 0.5)."""
+    ref, ours, r_all, o_all = _compare(ref_tools, synth.C2, tmp_path, reps=1, extra=extra)
     assert abs(ours - ref) <= 0.002, (ours, ref)
 
 

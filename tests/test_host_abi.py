@@ -55,9 +55,9 @@ def test_parse_argument_reference_semantics(lib):
     assert (b.param.ux, b.param.vy) == (4, 12) and b.model_path == "out.m"
     c = cm.parse_argument(["x", "--seed", "99", "--precision", "bf16sr", "-p", "te.bin", "tr"])
     assert c.param.seed == 99 and c.param.precision == "bf16sr" and c.va_path == "te.bin"
-    assert np.float32(c.param.hot_rows) == np.float32(0.5)  # copies of the most-rated rows by default
-    d = cm.parse_argument(["x", "--hot-rows", "0", "--deterministic", "3", "tr"])
-    assert d.param.hot_rows == 0 and d.param.deterministic == 3
+    assert c.param.hot_rows == 0  # no copies of the most-rated rows by default
+    d = cm.parse_argument(["x", "--hot-rows", "0.5", "--deterministic", "3", "tr"])
+    assert np.float32(d.param.hot_rows) == np.float32(0.5) and d.param.deterministic == 3
 
 
 @pytest.mark.parametrize("argv,msg", [
