@@ -1128,8 +1128,11 @@ def main():
         torch.cuda.synchronize()
         assert int(status.item()) == 0
         pms = p0.elapsed_time(p1) / 10
+        plain_gbs = samples_per_launch * BYTES_PER_SAMPLE[prec] / (pms * 1e-3) / 1e9
         plain = {"updates_per_sec": nnz / (pms * 1e-3), "ms_per_epoch": pms, "workers": workers, "epochs_timed": 10,
-                 "what": "the same device-resident epochs without row copies (--hot-rows 0), default L2 prefetch"}
+                 "achieved_gbs": plain_gbs, "l2_frac": plain_gbs / l2_gbs, "hbm_frac": plain_gbs / peak,
+                 "what": "the same device-resident epochs without row copies (the library's default, the "
+                         "reference's update), default L2 prefetch"}
         del d_R_plain
 
     hot_info = {"concurrency": conc, "per_copy": per_copy, "hot_users": hot.hot_users if hot else 0,
